@@ -1,0 +1,307 @@
+#!/usr/bin/env python3
+"""Benchmark: LULESH Sedov blast, plain FP64 Lagrange leapfrog at s=192.
+
+One "step" is one LULESH cycle (TimeIncrement + LagrangeLeapFrog) over the
+s=192 mesh (7,077,888 elements, 7,189,057 nodes) with LULESH 2.0 initial
+conditions.  The headline metric is zone-cycles per second (elements x
+cycles / time), the reference's own figure of merit.
+
+Legs of the default run (one JSON line on rank 0):
+  value        K cycles through the captured run-loop graph, state resident
+               in HBM; CUDA events on the library's stream
+  roofline     per-kernel device time of a kernel-by-kernel pass (CUDA
+               events between launches) against the kernel's algorithmic
+               bytes; HBM peak from MEASURED_PEAKS.json
+  e2e          the same cycles through the public C ABI with host buffers:
+               upload of the state from pinned memory, one
+               lulesh_time_increment + lulesh_lagrange_leapfrog call per cycle
+               with its status/scalar read-back, download of the final state
+  cpu_baseline the reference CPU implementation on this host's cores, a
+               bounded sample of the same workload
+
+``--impl reference`` times only the reference CPU implementation (the
+reference has no GPU path for this workload that runs on sm_103a).
+Multi-GPU (torchrun): every rank runs an independent replica (the step has no
+cross-instance exchange); ``value`` sums the replicas, timed by the slowest.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mzone-cycles/s: FP64 plain vs split-precision & batched, at ≤1e-6 origin-E err"
+UNIT = "Mzone-cycles/s"
+KERNELS = ("time_increment", "elem_force", "node_update", "elem_kinematics", "elem_material", "finalize")
+
+
+def algorithmic_bytes(ne: int, nn: int) -> dict:
+    """Compulsory DRAM bytes per launch of each kernel of the plain FP64 path
+    (8-byte doubles, 4-byte indices, every array touched once)."""
+    return {
+        "time_increment": 0,
+        # x,y,z,xd,yd,zd gathered (48/node), nodelist (32), p q v volo ss mass
+        # (48) in; stress + hourglass corner forces (2 x 24 doubles) out
+        "elem_force": 48 * nn + (32 + 48 + 384) * ne,
+        # corner slots (32/elem) + start (4/node), corner forces (384/elem),
+        # mass (8) + bc (1), x..zd read and written (96)
+        "node_update": (4 + 8 + 1 + 96) * nn + (32 + 384) * ne,
+        # nodelist, x..zd gathered, volo, v in; vnew delv arealg vdov delv_* delx_* out
+        "elem_kinematics": 48 * nn + (32 + 16 + 80) * ne,
+        # bc + 6 neighbour ids, delv_* delx_*, vnew volo vdov delv mass q v e p
+        # arealg in; p e q ss v out
+        "elem_material": (4 + 24 + 48 + 80 + 40) * ne,
+        "finalize": 0,
+    }
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return {**json.loads(p.read_text()), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(prefix="clocks_", suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.path.open("w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5], f[6], f[7], f[8]))
+            except ValueError:
+                continue
+        self.path.unlink(missing_ok=True)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for r in rows for n, v in zip(names, r[2:]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_run(s: int, warmup: int, cycles: int, threads: int) -> dict:
+    """Time the reference CPU implementation (built from its own sources by
+    build()) or, where it could not be built, the oracle port."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    exe, kind = (oracle.REF, "reference") if oracle.REF.exists() else (oracle.CLI, "port")
+    if not exe.exists():
+        oracle.build()
+        exe, kind = (oracle.REF, "reference") if oracle.REF.exists() else (oracle.CLI, "port")
+    if kind == "reference":
+        r = oracle.run_cli(exe, s, "v2", warmup + cycles, threads=threads, extra=["--warmup", str(warmup)])
+    else:
+        r = oracle.run_cli(exe, s, "v2", cycles, threads=threads, extra=["--warmup", str(warmup)])
+    return {"value": r["mzone_cycles_per_s"], "unit": UNIT, "cores": r["threads"], "kind": kind,
+            "elapsed_s": r["elapsed_s"], "cycles": r["timed_cycles"],
+            "sample": f"s={s} LULESH 2.0 initial conditions, {r['timed_cycles']} cycles after "
+                      f"{warmup} warm-up cycles, {r['threads']} OpenMP threads"}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def config_for(args, ne, nn) -> dict:
+    return {"workload": f"sedov_s{args.size}_{args.precision}", "s": args.size,
+            "elements": ne, "nodes": nn, "init": "LULESH 2.0 (e0=3.948746e7*(s/45)^3)",
+            "cycles_per_step": 1, "precision": args.precision,
+            "l2": "no flush: the state (~4.5 GB) is far larger than the 129 MB L2",
+            "parallelism": "replicas" if args.gpus > 1 else "single"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    ne, nn = args.size ** 3, (args.size + 1) ** 3
+    threads = os.cpu_count() or 1
+    n = max(1, min(args.steps, args.cpu_cycles))
+    cb = cpu_run(args.size, min(args.warmup, 2), n, threads)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": cb["cycles"], "warmup": min(args.warmup, 2),
+            "ms_per_step": 1e3 * cb["elapsed_s"] / max(cb["cycles"], 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_for(args, ne, nn),
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500, help="timed cycles")
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=192)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--profile-cycles", type=int, default=20)
+    ap.add_argument("--e2e-cycles", type=int, default=0, help="0: same as --steps")
+    ap.add_argument("--cpu-cycles", type=int, default=8, help="cycles of the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    precision = pkg.FP64 if args.precision == "fp64" else pkg.SPLIT
+
+    g = pkg.Lulesh(args.size, pkg.INIT_V2, precision)
+    ne, nn = g.num_elem, g.num_node
+    stream = torch.cuda.ExternalStream(g.stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- warm-up, then K cycles through the run-loop graph ----------------
+    assert g.run(args.warmup) == args.warmup
+    launches0 = g.kernel_launches
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        done = g.run(args.steps)
+        ev1.record(stream)
+        barrier()
+    ms = max_over_ranks(ev0.elapsed_time(ev1))
+    launches = g.kernel_launches - launches0
+    assert done == args.steps, (done, args.steps)
+    value = world * ne * args.steps / (ms * 1e-3) * 1e-6
+
+    # ---- per-kernel device times (kernel-by-kernel pass) ------------------
+    pc, kms = g.run_profiled(args.profile_cycles)
+    per_launch_ms = {k: v / max(pc, 1) for k, v in kms.items()}
+    abytes = algorithmic_bytes(ne, nn)
+    peaks = measured_peaks()
+    top = max(("elem_force", "node_update", "elem_kinematics", "elem_material"), key=lambda k: per_launch_ms[k])
+    achieved = abytes[top] / (per_launch_ms[top] * 1e-3) * 1e-9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        t = json.loads(tf.read_text()).get(args.precision, {}).get(top)
+        if t:
+            traffic = t["bytes_per_elem"] * ne
+    roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": abytes[top]}
+    cycle_bytes = sum(abytes.values())
+    total_ms = sum(per_launch_ms.values())
+    fp64_peak = pkg.probe_fp64_peak()
+    kernels = {k: {"ms": per_launch_ms[k], "share": per_launch_ms[k] / total_ms,
+                   "gbs": abytes[k] / (per_launch_ms[k] * 1e-3) * 1e-9 if per_launch_ms[k] > 0 else 0.0}
+               for k in KERNELS}
+
+    # ---- end to end through the C ABI with host buffers -------------------
+    e2e_cycles = args.e2e_cycles or args.steps
+    pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    host = pkg.Domain.empty(ne, nn, pinned=pin)
+    g.download(host)
+    state_bytes = sum(a.nbytes for a in host.arrays())
+    scalar_bytes = 40   # lulesh_scalars-sized status read per call
+    barrier()
+    t0 = time.perf_counter()
+    g.upload(host)
+    for _ in range(e2e_cycles):
+        g.time_increment()
+        g.lagrange_leapfrog()
+    g.download(host)
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * ne * e2e_cycles / e2e_s * 1e-6
+    e2e = {"value": e2e_value, "unit": UNIT, "cycles": e2e_cycles,
+           "h2d_bytes_per_step": state_bytes / e2e_cycles,
+           "d2h_bytes_per_step": (state_bytes + 2 * scalar_bytes * e2e_cycles) / e2e_cycles,
+           "timer": "host wall clock around upload + per-cycle ABI calls + download"}
+    origin_e = g.origin_energy()
+    g.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_run(args.size, 2, args.cpu_cycles, os.cpu_count() or 1)
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config_for(args, ne, nn), "roofline": roofline,
+                "fp64": {"peak_tflops_probe": fp64_peak,
+                         "note": "the FP64 pipe, not HBM, bounds this path: see kernels[*].gbs"},
+                "bytes_per_zone_cycle": cycle_bytes / ne,
+                "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clocks.summary(), "origin_energy_after": origin_e}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,194 @@
+/*
+ * lulesh_gb300.h -- C ABI of the GB300-native LULESH Lagrange leapfrog step.
+ *
+ * This is the drop-in boundary for the hot path of tmcdonell/lulesh-accelerate:
+ * the step API of src/LULESH.hs (lulesh :37-53, lagrangeLeapFrog :66-102,
+ * timeIncrement :1166-1213) over the Domain record of src/Domain.hs:11-21,
+ * with the semantics of the reference CPU implementation
+ * reference/C/LULESH-OMP.cc.  The Haskell host binds it with
+ * `foreign import ccall` in the same way src/VisIt.hs:71-86 binds
+ * cbits/visit.cc:149-177 (one `double*` per structure-of-arrays component);
+ * a C driver links it directly.  Nothing in these signatures is a C++, CUDA
+ * or PyTorch type.
+ *
+ * Conventions
+ *   - Node arrays have (s+1)^3 entries, element arrays s^3, both in the
+ *     reference's linear order: node (plane*(s+1)+row)*(s+1)+col, element
+ *     (plane*s+row)*s+col, col fastest (LULESH-OMP.cc:2996-3042).
+ *   - Host arrays belong to the caller and are only read or written during
+ *     the call (the touchArrayData idiom of src/VisIt.hs:43-48).
+ *   - Device memory, the CUDA stream and the captured CUDA graphs belong to
+ *     the context.  A context is used by one host thread at a time.
+ *   - Every call returns LULESH_OK (0) or a negative status.  VolumeError and
+ *     QStopError keep the reference's values (LULESH-OMP.cc:82); where the
+ *     reference calls exit(), the library returns the code instead.
+ *   - Calls that advance the state are ordered on the context's stream and
+ *     return only after it has drained, so that their status is final.
+ */
+#ifndef LULESH_GB300_H
+#define LULESH_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define LULESH_OK            0
+#define LULESH_VOLUME_ERROR (-1)   /* LULESH-OMP.cc:82 VolumeError */
+#define LULESH_QSTOP_ERROR  (-2)   /* LULESH-OMP.cc:82 QStopError  */
+#define LULESH_ERR_CUDA     (-3)   /* a CUDA call failed; see lulesh_last_error */
+#define LULESH_ERR_TIMEOUT  (-4)   /* a bounded device wait ran out */
+#define LULESH_ERR_ARG      (-5)   /* bad argument */
+
+/* ---- precision of the element kernels -------------------------------- */
+#define LULESH_PRECISION_FP64  0   /* plain FP64, the drop-in */
+#define LULESH_PRECISION_SPLIT 1   /* FP32 geometry/forces/Q gradients, FP64 state */
+
+/* ---- initial conditions of the Sedov problem ------------------------- */
+#define LULESH_INIT_V1 1           /* e(0)=3.948746e7, dt0=1e-7 (LULESH-OMP.cc:3053,3112) */
+#define LULESH_INIT_V2 2           /* e(0)=3.948746e7*(s/45)^3,
+                                      dt0=0.5*cbrt(volo(0))/sqrt(2*e0)
+                                      (lulesh-2.0.3/lulesh-init.cc:171-182) */
+
+/* Problem constants: the Parameters record of src/Domain.hs:23-53 with the
+ * values of the C reference (LULESH-OMP.cc:3051-3087). */
+typedef struct lulesh_params {
+    double e_cut, p_cut, q_cut, v_cut, u_cut;
+    double hgcoef, ss4o3, qstop, monoq_max_slope, monoq_limiter_mult;
+    double qlc_monoq, qqc_monoq, qqc;
+    double eosvmax, eosvmin, pmin, emin, dvovmax, refdens;
+    double dtfixed, deltatimemultlb, deltatimemultub, dtmax, stoptime;
+} lulesh_params;
+
+/* Scalar part of the Domain: the Scalar Time fields of src/Domain.hs:19-20
+ * plus the constraint and cycle state of the C reference
+ * (LULESH-OMP.cc:496-503). */
+typedef struct lulesh_scalars {
+    double time;
+    double deltatime;
+    double dtcourant;
+    double dthydro;
+    int cycle;
+} lulesh_scalars;
+
+/* Host description of a Sedov mesh.  Every pointer is caller-owned and may be
+ * NULL (that array is then not produced).  Sizes: node arrays num_node,
+ * element arrays num_elem, nodelist and node_elem_corner_list 8*num_elem. */
+typedef struct lulesh_mesh_view {
+    double *x, *y, *z;                       /* coordinates             */
+    double *volo, *elem_mass, *nodal_mass;   /* reference volume, masses */
+    int *nodelist;                           /* 8 node ids per element   */
+    int *node_elem_start, *node_elem_count;  /* node -> corner index     */
+    int *node_elem_corner_list;              /* entries 8*elem+corner    */
+    int *lxim, *lxip, *letam, *letap, *lzetam, *lzetap;  /* face neighbours */
+    int *elem_bc;                            /* boundary-condition bits  */
+    double e0;                               /* out: energy of element 0 */
+    double dt0;                              /* out: initial time step   */
+} lulesh_mesh_view;
+
+typedef struct lulesh_ctx lulesh_ctx;
+
+/* Fill *p with the reference constants (LULESH-OMP.cc:3051-3087). */
+void lulesh_default_params(lulesh_params *p);
+
+/* Element and node counts of the s^3 mesh. */
+int lulesh_mesh_sizes(int s, long *num_elem, long *num_node);
+
+/* Build the Sedov cube on the host exactly as the reference's main() does
+ * (LULESH-OMP.cc:2996-3171; node-to-corner lists as AllocateNodeElemIndexes
+ * :209-268).  Needs no GPU. */
+int lulesh_mesh_build(int s, int init_mode, lulesh_mesh_view *out);
+
+/* Create a context for an s^3 Sedov problem on the current CUDA device,
+ * build the mesh, upload it and set the initial state (replaces the
+ * initialisation of LULESH-OMP.cc main() :2960-3171 and src/Main.hs:60-83).
+ * params may be NULL for the reference constants. */
+int lulesh_create(int s, int init_mode, int precision, const lulesh_params *params,
+                  lulesh_ctx **out);
+void lulesh_destroy(lulesh_ctx *ctx);
+
+/* Message of the last failing call on this context (static storage when ctx
+ * is NULL). */
+const char *lulesh_last_error(const lulesh_ctx *ctx);
+
+/* ---- the Domain record (src/Domain.hs:11-21) ------------------------- */
+/* Upload / download the evolving state: position (x,y,z), velocity
+ * (xd,yd,zd), energy, pressure, viscosity, relative volume, sound speed
+ * and the two Scalar Time fields.  Any array pointer may be NULL to skip it. */
+int lulesh_upload_domain(lulesh_ctx *ctx,
+                         const double *x, const double *y, const double *z,
+                         const double *xd, const double *yd, const double *zd,
+                         const double *e, const double *p, const double *q,
+                         const double *v, const double *ss,
+                         double time, double deltatime);
+int lulesh_download_domain(lulesh_ctx *ctx,
+                           double *x, double *y, double *z,
+                           double *xd, double *yd, double *zd,
+                           double *e, double *p, double *q,
+                           double *v, double *ss,
+                           double *time, double *deltatime);
+
+/* Scalars, including dtcourant/dthydro/cycle (checkpoint/restart). */
+int lulesh_get_scalars(lulesh_ctx *ctx, lulesh_scalars *out);
+int lulesh_set_scalars(lulesh_ctx *ctx, const lulesh_scalars *in);
+
+/* Any named field, by the reference's accessor name (LULESH-OMP.cc:278-389):
+ * nodal "x" "y" "z" "xd" "yd" "zd" "fx" "fy" "fz" "nodalMass"; element "e"
+ * "p" "q" "ql" "qq" "v" "volo" "vnew" "delv" "vdov" "arealg" "ss" "elemMass"
+ * "delv_xi" "delv_eta" "delv_zeta" "delx_xi" "delx_eta" "delx_zeta".
+ * n must equal the field's length.  "fx/fy/fz" hold the nodal forces of the
+ * last LagrangeNodal only when the context keeps them (lulesh_keep_forces). */
+int lulesh_get_field(lulesh_ctx *ctx, const char *name, double *host, long n);
+int lulesh_set_field(lulesh_ctx *ctx, const char *name, const double *host, long n);
+int lulesh_keep_forces(lulesh_ctx *ctx, int keep);
+/* Change problem constants (e.g. qstop) of an existing context. */
+int lulesh_set_params(lulesh_ctx *ctx, const lulesh_params *params);
+int lulesh_get_params(lulesh_ctx *ctx, lulesh_params *params);
+
+/* ---- the step API ---------------------------------------------------- */
+int lulesh_time_increment(lulesh_ctx *ctx);        /* TimeIncrement      LULESH-OMP.cc:557-604   */
+int lulesh_lagrange_nodal(lulesh_ctx *ctx);        /* LagrangeNodal      LULESH-OMP.cc:1685-1704 */
+int lulesh_lagrange_elements(lulesh_ctx *ctx);     /* LagrangeElements   LULESH-OMP.cc:2784-2797 */
+int lulesh_calc_time_constraints(lulesh_ctx *ctx); /* CalcTimeConstraintsForElems :2935-2942   */
+int lulesh_lagrange_leapfrog(lulesh_ctx *ctx);     /* LagrangeLeapFrog   LULESH-OMP.cc:2944-2958;
+                                                      lagrangeLeapFrog   src/LULESH.hs:66-102     */
+
+/* The reference's main loop (LULESH-OMP.cc:3179-3188; src/Main.hs:90-108):
+ * while (time < stoptime) { TimeIncrement; LagrangeLeapFrog }, at most
+ * max_cycles cycles (max_cycles <= 0: no cap).  The loop runs on the device
+ * inside one CUDA graph; the host does not wait per cycle. */
+int lulesh_run(lulesh_ctx *ctx, int max_cycles, int *cycles_done);
+
+/* Result checks of LULESH-OMP.cc:3197-3223 / src/Main.hs:132-156. */
+int lulesh_origin_energy(lulesh_ctx *ctx, double *e0);
+int lulesh_symmetry(lulesh_ctx *ctx, double *max_abs_diff, double *total_abs_diff,
+                    double *max_rel_diff);
+
+/* Sizes of this context's mesh. */
+int lulesh_sizes(lulesh_ctx *ctx, int *s, long *num_elem, long *num_node);
+
+/* The context's cudaStream_t (as void*), for callers that time or order
+ * their own work against the library. */
+void *lulesh_stream(lulesh_ctx *ctx);
+
+/* Number of kernels this context has launched so far (graph replays count
+ * each kernel node).  Lets a caller check that the GPU path ran. */
+long long lulesh_kernel_launches(lulesh_ctx *ctx);
+
+/* ---- measurement helpers (no counterpart in the reference) ----------- */
+/* The same loop as lulesh_run, launched kernel by kernel with a CUDA event
+ * between kernels and one host synchronisation per cycle.  kernel_ms[i]
+ * receives the summed device time of kernel i over all cycles, in the order
+ * time increment, element force, node update, element kinematics, element
+ * material, constraint publication (LULESH_NUM_TIMED_KERNELS entries). */
+#define LULESH_NUM_TIMED_KERNELS 6
+int lulesh_run_profiled(lulesh_ctx *ctx, int max_cycles, int *cycles_done, double *kernel_ms);
+
+/* Measured FP64 fused-multiply-add throughput of the current device in
+ * TFLOP/s (2 flops per FMA), from a register-only kernel. */
+int lulesh_probe_fp64_peak(double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,385 @@
+"""GB300-native LULESH Lagrange leapfrog step: Python host interface.
+
+A thin ctypes layer over the C ABI of ``liblulesh_gb300.so``
+(``include/lulesh_gb300.h``).  It mirrors the reference's step API:
+
+* :class:`Parameters` -- the ``Parameters`` record (src/Domain.hs:23-82) with
+  the C reference's constants (reference/C/LULESH-OMP.cc:3051-3087);
+* :class:`Domain` -- the ``Domain`` record (src/Domain.hs:11-21): position,
+  velocity, energy, pressure, viscosity, relative volume, sound speed, time
+  and time step;
+* :class:`Lulesh` -- one problem on the GPU with ``time_increment``
+  (TimeIncrement, LULESH-OMP.cc:557-604), ``lagrange_leapfrog``
+  (LagrangeLeapFrog, :2944-2958) and its phases, and ``run`` (the main loop,
+  :3179-3188);
+* :func:`lulesh` -- the functional step of src/LULESH.hs:37-53 over host
+  arrays.
+
+Errors of the physics raise :class:`VolumeError` / :class:`QStopError`
+(the reference's exit codes -1 / -2, LULESH-OMP.cc:82).  There is no CPU
+fallback: without the built library or a CUDA device every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+__all__ = [
+    "Parameters", "Domain", "Scalars", "Lulesh", "lulesh", "library_path", "load_library",
+    "LuleshError", "VolumeError", "QStopError", "mesh_build", "mesh_sizes", "default_parameters",
+    "INIT_V1", "INIT_V2", "FP64", "SPLIT",
+]
+
+_PKG = Path(__file__).resolve().parent
+LIB_NAME = "liblulesh_gb300.so"
+
+OK, VOLUME_ERROR, QSTOP_ERROR, ERR_CUDA, ERR_TIMEOUT, ERR_ARG = 0, -1, -2, -3, -4, -5
+FP64, SPLIT = 0, 1
+INIT_V1, INIT_V2 = 1, 2
+
+
+class LuleshError(RuntimeError):
+    """A failing call of the library; ``code`` is its status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class VolumeError(LuleshError):
+    """An element volume became non-positive (reference exit code -1)."""
+
+
+class QStopError(LuleshError):
+    """Artificial viscosity exceeded qstop (reference exit code -2)."""
+
+
+class Parameters(C.Structure):
+    """``lulesh_params``: the constants of src/Domain.hs:23-53."""
+
+    _fields_ = [(n, C.c_double) for n in (
+        "e_cut", "p_cut", "q_cut", "v_cut", "u_cut",
+        "hgcoef", "ss4o3", "qstop", "monoq_max_slope", "monoq_limiter_mult",
+        "qlc_monoq", "qqc_monoq", "qqc",
+        "eosvmax", "eosvmin", "pmin", "emin", "dvovmax", "refdens",
+        "dtfixed", "deltatimemultlb", "deltatimemultub", "dtmax", "stoptime")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Scalars(C.Structure):
+    """``lulesh_scalars``: time, time step, constraint state and cycle."""
+
+    _fields_ = [("time", C.c_double), ("deltatime", C.c_double), ("dtcourant", C.c_double),
+                ("dthydro", C.c_double), ("cycle", C.c_int)]
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class MeshView(C.Structure):
+    _fields_ = [("x", _dp), ("y", _dp), ("z", _dp), ("volo", _dp), ("elem_mass", _dp),
+                ("nodal_mass", _dp), ("nodelist", _ip), ("node_elem_start", _ip),
+                ("node_elem_count", _ip), ("node_elem_corner_list", _ip),
+                ("lxim", _ip), ("lxip", _ip), ("letam", _ip), ("letap", _ip),
+                ("lzetam", _ip), ("lzetap", _ip), ("elem_bc", _ip),
+                ("e0", C.c_double), ("dt0", C.c_double)]
+
+
+_SIGNATURES = {
+    "lulesh_default_params": (None, [C.POINTER(Parameters)]),
+    "lulesh_mesh_sizes": (C.c_int, [C.c_int, C.POINTER(C.c_long), C.POINTER(C.c_long)]),
+    "lulesh_mesh_build": (C.c_int, [C.c_int, C.c_int, C.POINTER(MeshView)]),
+    "lulesh_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(Parameters), C.POINTER(C.c_void_p)]),
+    "lulesh_destroy": (None, [C.c_void_p]),
+    "lulesh_last_error": (C.c_char_p, [C.c_void_p]),
+    "lulesh_upload_domain": (C.c_int, [C.c_void_p] + [_dp] * 11 + [C.c_double, C.c_double]),
+    "lulesh_download_domain": (C.c_int, [C.c_void_p] + [_dp] * 13),
+    "lulesh_get_scalars": (C.c_int, [C.c_void_p, C.POINTER(Scalars)]),
+    "lulesh_set_scalars": (C.c_int, [C.c_void_p, C.POINTER(Scalars)]),
+    "lulesh_get_field": (C.c_int, [C.c_void_p, C.c_char_p, _dp, C.c_long]),
+    "lulesh_set_field": (C.c_int, [C.c_void_p, C.c_char_p, _dp, C.c_long]),
+    "lulesh_keep_forces": (C.c_int, [C.c_void_p, C.c_int]),
+    "lulesh_set_params": (C.c_int, [C.c_void_p, C.POINTER(Parameters)]),
+    "lulesh_get_params": (C.c_int, [C.c_void_p, C.POINTER(Parameters)]),
+    "lulesh_time_increment": (C.c_int, [C.c_void_p]),
+    "lulesh_lagrange_nodal": (C.c_int, [C.c_void_p]),
+    "lulesh_lagrange_elements": (C.c_int, [C.c_void_p]),
+    "lulesh_calc_time_constraints": (C.c_int, [C.c_void_p]),
+    "lulesh_lagrange_leapfrog": (C.c_int, [C.c_void_p]),
+    "lulesh_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "lulesh_origin_energy": (C.c_int, [C.c_void_p, _dp]),
+    "lulesh_symmetry": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "lulesh_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_long), C.POINTER(C.c_long)]),
+    "lulesh_stream": (C.c_void_p, [C.c_void_p]),
+    "lulesh_kernel_launches": (C.c_longlong, [C.c_void_p]),
+    "lulesh_run_profiled": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),
+    "lulesh_probe_fp64_peak": (C.c_int, [_dp]),
+}
+
+TIMED_KERNELS = ("time_increment", "elem_force", "node_update", "elem_kinematics",
+                 "elem_material", "finalize")
+
+_lib = None
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("LULESH_GB300_LIB", _PKG / LIB_NAME))
+
+
+def load_library():
+    """Load ``liblulesh_gb300.so`` (built by ``build.py``); raise if absent."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not path.exists():
+            raise LuleshError(ERR_ARG, f"{path} is not built: run lulesh-accelerate_gb300/build.py")
+        lib = C.CDLL(str(path))
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _ptr(a: np.ndarray | None, ctype=C.c_double):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def _check(rc: int, handle=None):
+    if rc == OK:
+        return
+    msg = load_library().lulesh_last_error(handle).decode(errors="replace")
+    if rc == VOLUME_ERROR:
+        raise VolumeError(rc, msg)
+    if rc == QSTOP_ERROR:
+        raise QStopError(rc, msg)
+    raise LuleshError(rc, msg)
+
+
+def default_parameters() -> Parameters:
+    p = Parameters()
+    load_library().lulesh_default_params(C.byref(p))
+    return p
+
+
+def mesh_sizes(s: int) -> tuple[int, int]:
+    ne, nn = C.c_long(), C.c_long()
+    _check(load_library().lulesh_mesh_sizes(s, C.byref(ne), C.byref(nn)))
+    return ne.value, nn.value
+
+
+def mesh_build(s: int, init: int = INIT_V2) -> dict:
+    """Host-built Sedov mesh (no GPU needed), as numpy arrays."""
+    ne, nn = mesh_sizes(s)
+    out = {k: np.zeros(nn) for k in ("x", "y", "z", "nodal_mass")}
+    out.update({k: np.zeros(ne) for k in ("volo", "elem_mass")})
+    out.update({k: np.zeros(8 * ne, np.int32) for k in ("nodelist", "node_elem_corner_list")})
+    out.update({k: np.zeros(nn, np.int32) for k in ("node_elem_start", "node_elem_count")})
+    out.update({k: np.zeros(ne, np.int32) for k in
+                ("lxim", "lxip", "letam", "letap", "lzetam", "lzetap", "elem_bc")})
+    mv = MeshView()
+    for name, _ in MeshView._fields_:
+        if name in out:
+            setattr(mv, name, _ptr(out[name], C.c_int if out[name].dtype == np.int32 else C.c_double))
+    _check(load_library().lulesh_mesh_build(s, init, C.byref(mv)))
+    out["e0"], out["dt0"] = mv.e0, mv.dt0
+    return out
+
+
+@dataclass
+class Domain:
+    """The evolving state of src/Domain.hs:11-21, structure of arrays."""
+
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    xd: np.ndarray
+    yd: np.ndarray
+    zd: np.ndarray
+    e: np.ndarray
+    p: np.ndarray
+    q: np.ndarray
+    v: np.ndarray
+    ss: np.ndarray
+    time: float = 0.0
+    deltatime: float = 0.0
+
+    NODE_FIELDS = ("x", "y", "z", "xd", "yd", "zd")
+    ELEM_FIELDS = ("e", "p", "q", "v", "ss")
+
+    @classmethod
+    def empty(cls, ne: int, nn: int, pinned=None) -> "Domain":
+        alloc = pinned or (lambda n: np.empty(n))
+        return cls(**{k: alloc(nn) for k in cls.NODE_FIELDS}, **{k: alloc(ne) for k in cls.ELEM_FIELDS})
+
+    def arrays(self):
+        return [getattr(self, k) for k in self.NODE_FIELDS + self.ELEM_FIELDS]
+
+
+NODE_FIELDS = {"x", "y", "z", "xd", "yd", "zd", "fx", "fy", "fz", "nodalMass"}
+
+
+class Lulesh:
+    """One Sedov problem resident on the current CUDA device.
+
+    ``init`` is ``INIT_V1`` (LULESH 1.0 initial energy and time step) or
+    ``INIT_V2`` (LULESH 2.0's scaled energy and analytic time step);
+    ``precision`` is ``FP64`` (the drop-in) or ``SPLIT``.
+    """
+
+    def __init__(self, s: int, init: int = INIT_V2, precision: int = FP64,
+                 params: Parameters | None = None):
+        lib = load_library()
+        h = C.c_void_p()
+        rc = lib.lulesh_create(s, init, precision, C.byref(params) if params is not None else None,
+                               C.byref(h))
+        _check(rc)
+        self._h = h
+        self.s = s
+        self.num_elem, self.num_node = mesh_sizes(s)
+
+    # lifetime -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().lulesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # step API ------------------------------------------------------------
+    def time_increment(self):
+        _check(load_library().lulesh_time_increment(self._h), self._h)
+
+    def lagrange_nodal(self):
+        _check(load_library().lulesh_lagrange_nodal(self._h), self._h)
+
+    def lagrange_elements(self):
+        _check(load_library().lulesh_lagrange_elements(self._h), self._h)
+
+    def calc_time_constraints(self):
+        _check(load_library().lulesh_calc_time_constraints(self._h), self._h)
+
+    def lagrange_leapfrog(self):
+        _check(load_library().lulesh_lagrange_leapfrog(self._h), self._h)
+
+    def run(self, max_cycles: int = 0) -> int:
+        """The reference main loop; returns the number of cycles done."""
+        n = C.c_int()
+        _check(load_library().lulesh_run(self._h, max_cycles, C.byref(n)), self._h)
+        return n.value
+
+    def run_profiled(self, max_cycles: int = 0) -> tuple[int, dict]:
+        """The main loop kernel by kernel; returns (cycles, summed ms per kernel)."""
+        n = C.c_int()
+        ms = np.zeros(len(TIMED_KERNELS))
+        _check(load_library().lulesh_run_profiled(self._h, max_cycles, C.byref(n), _ptr(ms)), self._h)
+        return n.value, dict(zip(TIMED_KERNELS, ms.tolist()))
+
+    # state ---------------------------------------------------------------
+    def _len(self, name: str) -> int:
+        return self.num_node if name in NODE_FIELDS else self.num_elem
+
+    def get_field(self, name: str) -> np.ndarray:
+        out = np.empty(self._len(name))
+        _check(load_library().lulesh_get_field(self._h, name.encode(), _ptr(out), out.size), self._h)
+        return out
+
+    def set_field(self, name: str, values) -> None:
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        _check(load_library().lulesh_set_field(self._h, name.encode(), _ptr(a), a.size), self._h)
+
+    def keep_forces(self, keep: bool = True):
+        _check(load_library().lulesh_keep_forces(self._h, int(keep)), self._h)
+
+    @property
+    def params(self) -> Parameters:
+        p = Parameters()
+        _check(load_library().lulesh_get_params(self._h, C.byref(p)), self._h)
+        return p
+
+    @params.setter
+    def params(self, p: Parameters):
+        _check(load_library().lulesh_set_params(self._h, C.byref(p)), self._h)
+
+    @property
+    def scalars(self) -> Scalars:
+        sc = Scalars()
+        _check(load_library().lulesh_get_scalars(self._h, C.byref(sc)), self._h)
+        return sc
+
+    @scalars.setter
+    def scalars(self, sc: Scalars):
+        _check(load_library().lulesh_set_scalars(self._h, C.byref(sc)), self._h)
+
+    def upload(self, dom: Domain):
+        a = [np.ascontiguousarray(v, dtype=np.float64) for v in dom.arrays()]
+        _check(load_library().lulesh_upload_domain(self._h, *[_ptr(v) for v in a],
+                                                   float(dom.time), float(dom.deltatime)), self._h)
+
+    def download(self, into: Domain | None = None) -> Domain:
+        dom = into or Domain.empty(self.num_elem, self.num_node)
+        t, dt = C.c_double(), C.c_double()
+        _check(load_library().lulesh_download_domain(self._h, *[_ptr(v) for v in dom.arrays()],
+                                                     C.byref(t), C.byref(dt)), self._h)
+        dom.time, dom.deltatime = t.value, dt.value
+        return dom
+
+    def origin_energy(self) -> float:
+        e = C.c_double()
+        _check(load_library().lulesh_origin_energy(self._h, C.byref(e)), self._h)
+        return e.value
+
+    def symmetry(self) -> tuple[float, float, float]:
+        """(MaxAbsDiff, TotalAbsDiff, MaxRelDiff) of energy plane 0."""
+        a, t, r = C.c_double(), C.c_double(), C.c_double()
+        _check(load_library().lulesh_symmetry(self._h, C.byref(a), C.byref(t), C.byref(r)), self._h)
+        return a.value, t.value, r.value
+
+    @property
+    def stream(self) -> int:
+        return load_library().lulesh_stream(self._h) or 0
+
+    @property
+    def kernel_launches(self) -> int:
+        return load_library().lulesh_kernel_launches(self._h)
+
+
+def probe_fp64_peak() -> float:
+    """Measured FP64 FMA throughput of the current device, TFLOP/s."""
+    t = C.c_double()
+    _check(load_library().lulesh_probe_fp64_peak(C.byref(t)))
+    return t.value
+
+
+def lulesh(ctx: Lulesh, dom: Domain) -> Domain:
+    """The functional step of src/LULESH.hs:37-53 over host arrays.
+
+    Uploads ``dom``, advances one cycle in the C reference's order
+    (TimeIncrement, then LagrangeLeapFrog) and returns the new state.  The
+    reference volumes and masses (``v0``, ``mN0`` of the Haskell API) are the
+    ones ``ctx`` was built with.
+    """
+    ctx.upload(dom)
+    ctx.time_increment()
+    ctx.lagrange_leapfrog()
+    return ctx.download()

@@ -1,0 +1,199 @@
+// geometry.cuh -- per-element hexahedron geometry in FP64, device side.
+//
+// Each function keeps the floating-point association of the reference
+// routine it restates (reference/C/LULESH-OMP.cc, lines cited per function);
+// only multiply-add contraction, which nvcc applies by default, differs.
+#pragma once
+
+namespace lulesh {
+
+// Jacobian columns of one coordinate at the element centre, scaled by 1/8
+// (LULESH-OMP.cc:650-660).
+__device__ __forceinline__ void jac_column(const double c[8], double &xi, double &et, double &ze)
+{
+    const double d60 = c[6] - c[0], d53 = c[5] - c[3];
+    const double d71 = c[7] - c[1], d42 = c[4] - c[2];
+    xi = .125 * (((d60 + d53) - d71) - d42);
+    et = .125 * (((d60 - d53) + d71) - d42);
+    ze = .125 * (((d60 + d53) + d71) + d42);
+}
+
+// CalcElemShapeFunctionDerivatives (LULESH-OMP.cc:619-706): B for corners
+// 0..3 (4..7 are their negatives) and the Jacobian volume.
+__device__ __forceinline__ void shape_derivs4(const double x[8], const double y[8], const double z[8],
+                                              double b[3][4], double &volume)
+{
+    double a[3], t[3], c[3];
+    jac_column(x, a[0], t[0], c[0]);
+    jac_column(y, a[1], t[1], c[1]);
+    jac_column(z, a[2], t[2], c[2]);
+    double cxi[3], cet[3], cze[3];
+    cxi[0] = (t[1] * c[2]) - (t[2] * c[1]);
+    cxi[1] = (t[2] * c[0]) - (t[0] * c[2]);
+    cxi[2] = (t[0] * c[1]) - (t[1] * c[0]);
+    cet[0] = (a[2] * c[1]) - (a[1] * c[2]);
+    cet[1] = (a[0] * c[2]) - (a[2] * c[0]);
+    cet[2] = (a[1] * c[0]) - (a[0] * c[1]);
+    cze[0] = (a[1] * t[2]) - (a[2] * t[1]);
+    cze[1] = (a[2] * t[0]) - (a[0] * t[2]);
+    cze[2] = (a[0] * t[1]) - (a[1] * t[0]);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        b[d][0] = ((-cxi[d]) - cet[d]) - cze[d];
+        b[d][1] = (cxi[d] - cet[d]) - cze[d];
+        b[d][2] = (cxi[d] + cet[d]) - cze[d];
+        b[d][3] = ((-cxi[d]) + cet[d]) - cze[d];
+    }
+    volume = 8.0 * ((t[0] * cet[0] + t[1] * cet[1]) + t[2] * cet[2]);
+}
+
+// Jacobian volume only (the determinant IntegrateStressForElems checks).
+__device__ __forceinline__ double jacobian_volume(const double x[8], const double y[8], const double z[8])
+{
+    double a[3], t[3], c[3];
+    jac_column(x, a[0], t[0], c[0]);
+    jac_column(y, a[1], t[1], c[1]);
+    jac_column(z, a[2], t[2], c[2]);
+    const double cet0 = (a[2] * c[1]) - (a[1] * c[2]);
+    const double cet1 = (a[0] * c[2]) - (a[2] * c[0]);
+    const double cet2 = (a[1] * c[0]) - (a[0] * c[1]);
+    return 8.0 * ((t[0] * cet0 + t[1] * cet1) + t[2] * cet2);
+}
+
+// CalcElemNodeNormals + SumElemFaceNormal (LULESH-OMP.cc:708-799).  The six
+// faces are visited in the reference's order; each corner accumulates the
+// quarter-area vectors of its three faces in that order.
+__device__ __forceinline__ void face_area(const double x[8], const double y[8], const double z[8],
+                                          int n0, int n1, int n2, int n3,
+                                          double &ax, double &ay, double &az)
+{
+    const double bx0 = 0.5 * (((x[n3] + x[n2]) - x[n1]) - x[n0]);
+    const double by0 = 0.5 * (((y[n3] + y[n2]) - y[n1]) - y[n0]);
+    const double bz0 = 0.5 * (((z[n3] + z[n2]) - z[n1]) - z[n0]);
+    const double bx1 = 0.5 * (((x[n2] + x[n1]) - x[n3]) - x[n0]);
+    const double by1 = 0.5 * (((y[n2] + y[n1]) - y[n3]) - y[n0]);
+    const double bz1 = 0.5 * (((z[n2] + z[n1]) - z[n3]) - z[n0]);
+    ax = 0.25 * (by0 * bz1 - bz0 * by1);
+    ay = 0.25 * (bz0 * bx1 - bx0 * bz1);
+    az = 0.25 * (bx0 * by1 - by0 * bx1);
+}
+
+__device__ __forceinline__ void node_normals(double pf[3][8], const double x[8], const double y[8],
+                                             const double z[8])
+{
+    double a[6][3];
+    face_area(x, y, z, 0, 1, 2, 3, a[0][0], a[0][1], a[0][2]);
+    face_area(x, y, z, 0, 4, 5, 1, a[1][0], a[1][1], a[1][2]);
+    face_area(x, y, z, 1, 5, 6, 2, a[2][0], a[2][1], a[2][2]);
+    face_area(x, y, z, 2, 6, 7, 3, a[3][0], a[3][1], a[3][2]);
+    face_area(x, y, z, 3, 7, 4, 0, a[4][0], a[4][1], a[4][2]);
+    face_area(x, y, z, 4, 7, 6, 5, a[5][0], a[5][1], a[5][2]);
+    // faces touching each corner, ascending (= accumulation order)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        pf[d][0] = (a[0][d] + a[1][d]) + a[4][d];
+        pf[d][1] = (a[0][d] + a[1][d]) + a[2][d];
+        pf[d][2] = (a[0][d] + a[2][d]) + a[3][d];
+        pf[d][3] = (a[0][d] + a[3][d]) + a[4][d];
+        pf[d][4] = (a[1][d] + a[4][d]) + a[5][d];
+        pf[d][5] = (a[1][d] + a[2][d]) + a[5][d];
+        pf[d][6] = (a[2][d] + a[3][d]) + a[5][d];
+        pf[d][7] = (a[3][d] + a[4][d]) + a[5][d];
+    }
+}
+
+// VoluDer (LULESH-OMP.cc:978-1006) on six corners given by index.
+__device__ __forceinline__ void volu_der(const double x[8], const double y[8], const double z[8],
+                                         int i0, int i1, int i2, int i3, int i4, int i5,
+                                         double &dx, double &dy, double &dz)
+{
+    const double twelfth = 1.0 / 12.0;
+    const double x0 = x[i0], x1 = x[i1], x2 = x[i2], x3 = x[i3], x4 = x[i4], x5 = x[i5];
+    const double y0 = y[i0], y1 = y[i1], y2 = y[i2], y3 = y[i3], y4 = y[i4], y5 = y[i5];
+    const double z0 = z[i0], z1 = z[i1], z2 = z[i2], z3 = z[i3], z4 = z[i4], z5 = z[i5];
+    const double vx =
+        (y1 + y2) * (z0 + z1) - (y0 + y1) * (z1 + z2) +
+        (y0 + y4) * (z3 + z4) - (y3 + y4) * (z0 + z4) -
+        (y2 + y5) * (z3 + z5) + (y3 + y5) * (z2 + z5);
+    const double vy =
+        -(x1 + x2) * (z0 + z1) + (x0 + x1) * (z1 + z2) -
+        (x0 + x4) * (z3 + z4) + (x3 + x4) * (z0 + z4) +
+        (x2 + x5) * (z3 + z5) - (x3 + x5) * (z2 + z5);
+    const double vz =
+        -(y1 + y2) * (x0 + x1) + (y0 + y1) * (x1 + x2) -
+        (y0 + y4) * (x3 + x4) + (y3 + y4) * (x0 + x4) +
+        (y2 + y5) * (x3 + x5) - (y3 + y5) * (x2 + x5);
+    dx = vx * twelfth;
+    dy = vy * twelfth;
+    dz = vz * twelfth;
+}
+
+// CalcElemVolumeDerivative (LULESH-OMP.cc:1008-1048).
+__device__ __forceinline__ void volume_derivative(double dvdx[8], double dvdy[8], double dvdz[8],
+                                                  const double x[8], const double y[8], const double z[8])
+{
+    volu_der(x, y, z, 1, 2, 3, 4, 5, 7, dvdx[0], dvdy[0], dvdz[0]);
+    volu_der(x, y, z, 0, 1, 2, 7, 4, 6, dvdx[3], dvdy[3], dvdz[3]);
+    volu_der(x, y, z, 3, 0, 1, 6, 7, 5, dvdx[2], dvdy[2], dvdz[2]);
+    volu_der(x, y, z, 2, 3, 0, 5, 6, 4, dvdx[1], dvdy[1], dvdz[1]);
+    volu_der(x, y, z, 7, 6, 5, 0, 3, 1, dvdx[4], dvdy[4], dvdz[4]);
+    volu_der(x, y, z, 4, 7, 6, 1, 0, 2, dvdx[5], dvdy[5], dvdz[5]);
+    volu_der(x, y, z, 5, 4, 7, 2, 1, 3, dvdx[6], dvdy[6], dvdz[6]);
+    volu_der(x, y, z, 6, 5, 4, 3, 2, 0, dvdx[7], dvdy[7], dvdz[7]);
+}
+
+// CalcElemVolume (LULESH-OMP.cc:1706-1790).
+__device__ __forceinline__ double elem_volume(const double x[8], const double y[8], const double z[8])
+{
+    const double twelveth = 1.0 / 12.0;
+    const double dx61 = x[6] - x[1], dy61 = y[6] - y[1], dz61 = z[6] - z[1];
+    const double dx70 = x[7] - x[0], dy70 = y[7] - y[0], dz70 = z[7] - z[0];
+    const double dx63 = x[6] - x[3], dy63 = y[6] - y[3], dz63 = z[6] - z[3];
+    const double dx20 = x[2] - x[0], dy20 = y[2] - y[0], dz20 = z[2] - z[0];
+    const double dx50 = x[5] - x[0], dy50 = y[5] - y[0], dz50 = z[5] - z[0];
+    const double dx64 = x[6] - x[4], dy64 = y[6] - y[4], dz64 = z[6] - z[4];
+    const double dx31 = x[3] - x[1], dy31 = y[3] - y[1], dz31 = z[3] - z[1];
+    const double dx72 = x[7] - x[2], dy72 = y[7] - y[2], dz72 = z[7] - z[2];
+    const double dx43 = x[4] - x[3], dy43 = y[4] - y[3], dz43 = z[4] - z[3];
+    const double dx57 = x[5] - x[7], dy57 = y[5] - y[7], dz57 = z[5] - z[7];
+    const double dx14 = x[1] - x[4], dy14 = y[1] - y[4], dz14 = z[1] - z[4];
+    const double dx25 = x[2] - x[5], dy25 = y[2] - y[5], dz25 = z[2] - z[5];
+#define LULESH_TRIPLE(x1, y1, z1, x2, y2, z2, x3, y3, z3) \
+    ((x1) * ((y2) * (z3) - (z2) * (y3)) + (x2) * ((z1) * (y3) - (y1) * (z3)) + (x3) * ((y1) * (z2) - (z1) * (y2)))
+    const double vol =
+        LULESH_TRIPLE(dx31 + dx72, dx63, dx20, dy31 + dy72, dy63, dy20, dz31 + dz72, dz63, dz20) +
+        LULESH_TRIPLE(dx43 + dx57, dx64, dx70, dy43 + dy57, dy64, dy70, dz43 + dz57, dz64, dz70) +
+        LULESH_TRIPLE(dx14 + dx25, dx61, dx50, dy14 + dy25, dy61, dy50, dz14 + dz25, dz61, dz50);
+#undef LULESH_TRIPLE
+    return vol * twelveth;
+}
+
+// AreaFace (LULESH-OMP.cc:1799-1819).
+__device__ __forceinline__ double area_face(const double x[8], const double y[8], const double z[8],
+                                            int a, int b, int c, int d)
+{
+    const double fx = (x[c] - x[a]) - (x[d] - x[b]);
+    const double fy = (y[c] - y[a]) - (y[d] - y[b]);
+    const double fz = (z[c] - z[a]) - (z[d] - z[b]);
+    const double gx = (x[c] - x[a]) + (x[d] - x[b]);
+    const double gy = (y[c] - y[a]) + (y[d] - y[b]);
+    const double gz = (z[c] - z[a]) + (z[d] - z[b]);
+    const double fg = fx * gx + fy * gy + fz * gz;
+    return (fx * fx + fy * fy + fz * fz) * (gx * gx + gy * gy + gz * gz) - fg * fg;
+}
+
+// CalcElemCharacteristicLength (LULESH-OMP.cc:1821-1862).
+__device__ __forceinline__ double char_length(const double x[8], const double y[8], const double z[8],
+                                              double volume)
+{
+    double m = 0.0, a;
+    a = area_face(x, y, z, 0, 1, 2, 3); m = fmax(a, m);
+    a = area_face(x, y, z, 4, 5, 6, 7); m = fmax(a, m);
+    a = area_face(x, y, z, 0, 1, 5, 4); m = fmax(a, m);
+    a = area_face(x, y, z, 1, 2, 6, 5); m = fmax(a, m);
+    a = area_face(x, y, z, 2, 3, 7, 6); m = fmax(a, m);
+    a = area_face(x, y, z, 3, 0, 4, 7); m = fmax(a, m);
+    return 4.0 * volume / sqrt(m);
+}
+
+}  // namespace lulesh

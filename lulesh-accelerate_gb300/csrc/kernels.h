@@ -1,0 +1,31 @@
+// kernels.h -- launchers of the step kernels (host side of the .cu files).
+#pragma once
+
+#include "lulesh_internal.h"
+
+#include <cuda_runtime.h>
+
+namespace lulesh {
+
+// Threads per block of the element and node kernels.  The element kernels
+// are FP64-issue-bound; 128 threads keep the FP64 pipe busy with two to
+// four resident blocks per SM at their register counts.
+constexpr int kBlockElem = 128;
+constexpr int kBlockNode = 256;
+
+// Plain FP64 path (step_fp64.cu).
+void launch_time_increment(const Dom &d, cudaStream_t st);
+void launch_lagrange_nodal(const Dom &d, cudaStream_t st);
+void launch_lagrange_elements(const Dom &d, cudaStream_t st, bool with_constraints);
+void launch_time_constraints(const Dom &d, cudaStream_t st);
+void launch_finalize(const Dom &d, cudaStream_t st);
+void launch_run_prologue(const Dom &d, cudaStream_t st, const int *max_cycles,
+                         cudaGraphConditionalHandle h, int *active);
+void launch_run_body(const Dom &d, cudaStream_t st, cudaGraphConditionalHandle h, int *active);
+int kernels_per_cycle();
+constexpr int kRunCycleLimit = 1 << 26;
+constexpr int kTimedKernels = 6;   // time increment, force, node, kinematics, material, finalize
+void launch_cycle_timed(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTimedKernels + 1]);
+void launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t st);
+
+}  // namespace lulesh

@@ -1,0 +1,92 @@
+// lulesh_internal.h -- definitions shared by the host code and the kernels.
+#pragma once
+
+#include "../../include/lulesh_gb300.h"
+
+#include <cstdint>
+#include <vector>
+
+namespace lulesh {
+
+// Largest edge length: 8*s^3 corner indices must fit an int32
+// (Index_t is int in the reference, LULESH-OMP.cc:93).
+constexpr int kMaxEdge = 640;
+
+// Element boundary-condition bits (LULESH-OMP.cc:231-253).
+enum : int {
+    BC_XI_M = 0x003, BC_XI_M_SYMM = 0x001, BC_XI_M_FREE = 0x002,
+    BC_XI_P = 0x00c, BC_XI_P_SYMM = 0x004, BC_XI_P_FREE = 0x008,
+    BC_ETA_M = 0x030, BC_ETA_M_SYMM = 0x010, BC_ETA_M_FREE = 0x020,
+    BC_ETA_P = 0x0c0, BC_ETA_P_SYMM = 0x040, BC_ETA_P_FREE = 0x080,
+    BC_ZETA_M = 0x300, BC_ZETA_M_SYMM = 0x100, BC_ZETA_M_FREE = 0x200,
+    BC_ZETA_P = 0xc00, BC_ZETA_P_SYMM = 0x400, BC_ZETA_P_FREE = 0x800,
+};
+
+// Error words written by the kernels, in the reference's program order
+// within one cycle; the first non-zero word decides the status.
+enum ErrSite : int {
+    ERR_K1_DETERM = 0,   // IntegrateStressForElems determ <= 0   (LULESH-OMP.cc:1579-1584)
+    ERR_K1_VOLUME = 1,   // CalcHourglassControlForElems v <= 0   (:1541-1543)
+    ERR_K3_VNEW = 2,     // CalcLagrangeElements vnew <= 0        (:2026-2029)
+    ERR_K3_QSTOP = 3,    // CalcQForElems q > qstop              (:2369-2381)
+    ERR_K3_MATV = 4,     // ApplyMaterialPropertiesForElems v<=0  (:2750-2752)
+    ERR_NUM = 5
+};
+
+// Device-resident scalar state of one problem instance.
+struct DevScalars {
+    double time, deltatime, dtcourant, dthydro;
+    int cycle;
+    int err_any;                         // OR of err[]
+    int err[ERR_NUM];                    // first offending element + 1, 0 = none
+    int run_cycles;                      // cycles done by the current lulesh_run
+    int run_max;                         // its cap (<= 0: none)
+    int pad;
+    unsigned long long courant_key;      // order-preserving keys of the
+    unsigned long long hydro_key;        // constraint minima (see keys below)
+};
+
+// Host copy of the mesh (built in mesh.cpp).
+struct HostMesh {
+    int s = 0;
+    long ne = 0, nn = 0;
+    std::vector<double> x, y, z, volo, elem_mass, nodal_mass;
+    std::vector<int> nodelist, node_elem_start, node_elem_count, node_elem_corner_list;
+    std::vector<int> lxim, lxip, letam, letap, lzetam, lzetap, elem_bc;
+    std::vector<unsigned char> node_bc;  // bit0 x=0, bit1 y=0, bit2 z=0 plane
+    double e0 = 0.0, dt0 = 0.0;
+    void build(int s, int init_mode);
+};
+
+double host_elem_volume(const double x[8], const double y[8], const double z[8]);
+void default_params(lulesh_params *p);
+
+// Everything one kernel launch needs, passed by value.
+struct Dom {
+    int s, ne, nn;
+    int keep;                            // bit0: store nodal forces, bit1: store ql/qq
+    // mesh (read-only)
+    const int *nodelist;                 // [8*ne] element-major, as the reference
+    const int *corner_start;             // [nn+1]
+    const int *corner_list;              // [8*ne] corner-major slots c*ne+e
+    const unsigned char *node_bc;        // [nn]
+    const int *lxim, *lxip, *letam, *letap, *lzetam, *lzetap, *elem_bc;
+    const double *volo, *elem_mass, *nodal_mass;
+    // nodal state
+    double *x, *y, *z, *xd, *yd, *zd;
+    double *fx, *fy, *fz;                // only when keep & 1
+    // element state
+    double *e, *p, *q, *v, *ss;
+    double *vnew, *delv, *vdov, *arealg, *ql, *qq;
+    double *delv_xi, *delv_eta, *delv_zeta, *delx_xi, *delx_eta, *delx_zeta;
+    // corner forces, corner-major [8*ne]: stress and hourglass parts kept
+    // apart so that the node sums associate as the reference's do
+    double *fsx, *fsy, *fsz, *fhx, *fhy, *fhz;
+    // split-precision corner forces (float, corner-major [8*ne])
+    float *f32x, *f32y, *f32z;
+    DevScalars *sc;
+    const int *gate;                     // host-driven run loop: cycle runs while *gate != 0
+    lulesh_params prm;
+};
+
+}  // namespace lulesh

@@ -1,0 +1,239 @@
+// mesh.cpp -- host construction of the Sedov cube.
+//
+// Builds what the reference's main() builds before its time loop
+// (reference/C/LULESH-OMP.cc:2960-3171): coordinates, hexahedron
+// connectivity, node-to-corner lists (AllocateNodeElemIndexes :209-268),
+// reference volumes and masses, face neighbours, boundary-condition bits and
+// the initial energy / time step.  Compiled with -ffp-contract=off so that
+// the floating-point results are the reference's on every host architecture.
+#include "lulesh_internal.h"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace lulesh {
+
+// CalcElemVolume (LULESH-OMP.cc:1706-1790), same association as the
+// reference, for the host set-up.
+double host_elem_volume(const double x[8], const double y[8], const double z[8])
+{
+    const double twelveth = 1.0 / 12.0;
+    const double dx61 = x[6] - x[1], dy61 = y[6] - y[1], dz61 = z[6] - z[1];
+    const double dx70 = x[7] - x[0], dy70 = y[7] - y[0], dz70 = z[7] - z[0];
+    const double dx63 = x[6] - x[3], dy63 = y[6] - y[3], dz63 = z[6] - z[3];
+    const double dx20 = x[2] - x[0], dy20 = y[2] - y[0], dz20 = z[2] - z[0];
+    const double dx50 = x[5] - x[0], dy50 = y[5] - y[0], dz50 = z[5] - z[0];
+    const double dx64 = x[6] - x[4], dy64 = y[6] - y[4], dz64 = z[6] - z[4];
+    const double dx31 = x[3] - x[1], dy31 = y[3] - y[1], dz31 = z[3] - z[1];
+    const double dx72 = x[7] - x[2], dy72 = y[7] - y[2], dz72 = z[7] - z[2];
+    const double dx43 = x[4] - x[3], dy43 = y[4] - y[3], dz43 = z[4] - z[3];
+    const double dx57 = x[5] - x[7], dy57 = y[5] - y[7], dz57 = z[5] - z[7];
+    const double dx14 = x[1] - x[4], dy14 = y[1] - y[4], dz14 = z[1] - z[4];
+    const double dx25 = x[2] - x[5], dy25 = y[2] - y[5], dz25 = z[2] - z[5];
+    auto triple = [](double x1, double y1, double z1, double x2, double y2, double z2,
+                     double x3, double y3, double z3) {
+        return x1 * (y2 * z3 - z2 * y3) + x2 * (z1 * y3 - y1 * z3) + x3 * (y1 * z2 - z1 * y2);
+    };
+    double vol = triple(dx31 + dx72, dx63, dx20, dy31 + dy72, dy63, dy20, dz31 + dz72, dz63, dz20) +
+                 triple(dx43 + dx57, dx64, dx70, dy43 + dy57, dy64, dy70, dz43 + dz57, dz64, dz70) +
+                 triple(dx14 + dx25, dx61, dx50, dy14 + dy25, dy61, dy50, dz14 + dz25, dz61, dz50);
+    return vol * twelveth;
+}
+
+void default_params(lulesh_params *p)
+{
+    std::memset(p, 0, sizeof *p);
+    p->dtfixed = -1.0e-7;
+    p->deltatimemultlb = 1.1;
+    p->deltatimemultub = 1.2;
+    p->stoptime = 1.0e-2;
+    p->dtmax = 1.0e-2;
+    p->e_cut = 1.0e-7;
+    p->p_cut = 1.0e-7;
+    p->q_cut = 1.0e-7;
+    p->u_cut = 1.0e-7;
+    p->v_cut = 1.0e-10;
+    p->hgcoef = 3.0;
+    p->ss4o3 = 4.0 / 3.0;
+    p->qstop = 1.0e+12;
+    p->monoq_max_slope = 1.0;
+    p->monoq_limiter_mult = 2.0;
+    p->qlc_monoq = 0.5;
+    p->qqc_monoq = 2.0 / 3.0;
+    p->qqc = 2.0;
+    p->pmin = 0.0;
+    p->emin = -1.0e+15;
+    p->dvovmax = 0.1;
+    p->eosvmax = 1.0e+9;
+    p->eosvmin = 1.0e-9;
+    p->refdens = 1.0;
+}
+
+void HostMesh::build(int s_, int init_mode)
+{
+    s = s_;
+    const int en = s + 1;
+    ne = (long)s * s * s;
+    nn = (long)en * en * en;
+
+    x.assign(nn, 0.0);
+    y.assign(nn, 0.0);
+    z.assign(nn, 0.0);
+    long n = 0;
+    for (int pl = 0; pl < en; ++pl)
+        for (int row = 0; row < en; ++row)
+            for (int col = 0; col < en; ++col, ++n) {
+                // LULESH-OMP.cc:3001-3014: 1.125*(i)/s, exactly 0 on the first plane
+                x[n] = col ? 1.125 * double(col) / double(s) : 0.0;
+                y[n] = row ? 1.125 * double(row) / double(s) : 0.0;
+                z[n] = pl ? 1.125 * double(pl) / double(s) : 0.0;
+            }
+
+    nodelist.assign(8 * ne, 0);
+    long e = 0;
+    for (int pl = 0; pl < s; ++pl)
+        for (int row = 0; row < s; ++row)
+            for (int col = 0; col < s; ++col, ++e) {
+                const int n0 = (pl * en + row) * en + col;
+                int *l = &nodelist[8 * e];
+                l[0] = n0;
+                l[1] = n0 + 1;
+                l[2] = n0 + en + 1;
+                l[3] = n0 + en;
+                l[4] = n0 + en * en;
+                l[5] = n0 + en * en + 1;
+                l[6] = n0 + en * en + en + 1;
+                l[7] = n0 + en * en + en;
+            }
+
+    // node -> corner lists in (element, corner) order: a counting sort.
+    node_elem_count.assign(nn, 0);
+    node_elem_start.assign(nn, 0);
+    node_elem_corner_list.assign(8 * ne, 0);
+    for (long i = 0; i < 8 * ne; ++i) node_elem_count[nodelist[i]]++;
+    for (long i = 1; i < nn; ++i) node_elem_start[i] = node_elem_start[i - 1] + node_elem_count[i - 1];
+    std::vector<int> fill(nn, 0);
+    for (long i = 0; i < ne; ++i)
+        for (int j = 0; j < 8; ++j) {
+            const int m = nodelist[8 * i + j];
+            node_elem_corner_list[node_elem_start[m] + fill[m]++] = int(8 * i + j);
+        }
+
+    volo.assign(ne, 0.0);
+    elem_mass.assign(ne, 0.0);
+    nodal_mass.assign(nn, 0.0);
+    for (long i = 0; i < ne; ++i) {
+        double xl[8], yl[8], zl[8];
+        for (int k = 0; k < 8; ++k) {
+            const int g = nodelist[8 * i + k];
+            xl[k] = x[g];
+            yl[k] = y[g];
+            zl[k] = z[g];
+        }
+        const double vol = host_elem_volume(xl, yl, zl);
+        volo[i] = vol;
+        elem_mass[i] = vol;
+        for (int k = 0; k < 8; ++k) nodal_mass[nodelist[8 * i + k]] += vol / 8.0;
+    }
+
+    if (init_mode == LULESH_INIT_V2) {
+        // lulesh-2.0.3/lulesh-init.cc:171-182
+        const double ebase = 3.948746e+7;
+        const double scale = double(s) / 45.0;
+        e0 = ebase * scale * scale * scale;
+        dt0 = (.5 * std::cbrt(volo[0])) / std::sqrt(2.0 * e0);
+    } else {
+        e0 = 3.948746e+7;   // LULESH-OMP.cc:3112
+        dt0 = 1.0e-7;       // LULESH-OMP.cc:3053
+    }
+
+    // symmetry-plane node sets (LULESH-OMP.cc:3114-3125) as a per-node mask
+    node_bc.assign(nn, 0);
+    for (int i = 0; i < en; ++i)
+        for (int j = 0; j < en; ++j) {
+            node_bc[i * en * en + j * en] |= 1;  // symmX: x = 0 plane
+            node_bc[i * en * en + j] |= 2;       // symmY: y = 0 plane
+            node_bc[i * en + j] |= 4;            // symmZ: z = 0 plane
+        }
+
+    // face neighbours (LULESH-OMP.cc:3127-3151)
+    lxim.assign(ne, 0); lxip.assign(ne, 0);
+    letam.assign(ne, 0); letap.assign(ne, 0);
+    lzetam.assign(ne, 0); lzetap.assign(ne, 0);
+    lxim[0] = 0;
+    for (long i = 1; i < ne; ++i) { lxim[i] = int(i - 1); lxip[i - 1] = int(i); }
+    lxip[ne - 1] = int(ne - 1);
+    for (long i = 0; i < s; ++i) { letam[i] = int(i); letap[ne - s + i] = int(ne - s + i); }
+    for (long i = s; i < ne; ++i) { letam[i] = int(i - s); letap[i - s] = int(i); }
+    const long s2 = (long)s * s;
+    for (long i = 0; i < s2; ++i) { lzetam[i] = int(i); lzetap[ne - s2 + i] = int(ne - s2 + i); }
+    for (long i = s2; i < ne; ++i) { lzetam[i] = int(i - s2); lzetap[i - s2] = int(i); }
+
+    // boundary-condition bits (LULESH-OMP.cc:3153-3171)
+    elem_bc.assign(ne, 0);
+    for (long i = 0; i < s; ++i) {
+        const long pinc = i * s2, rinc = i * s;
+        for (long j = 0; j < s; ++j) {
+            elem_bc[pinc + j * s] |= BC_XI_M_SYMM;
+            elem_bc[pinc + j * s + s - 1] |= BC_XI_P_FREE;
+            elem_bc[pinc + j] |= BC_ETA_M_SYMM;
+            elem_bc[pinc + j + s2 - s] |= BC_ETA_P_FREE;
+            elem_bc[rinc + j] |= BC_ZETA_M_SYMM;
+            elem_bc[rinc + j + ne - s2] |= BC_ZETA_P_FREE;
+        }
+    }
+}
+
+}  // namespace lulesh
+
+extern "C" {
+
+void lulesh_default_params(lulesh_params *p)
+{
+    if (p) lulesh::default_params(p);
+}
+
+int lulesh_mesh_sizes(int s, long *num_elem, long *num_node)
+{
+    if (s < 1 || s > lulesh::kMaxEdge) return LULESH_ERR_ARG;
+    if (num_elem) *num_elem = (long)s * s * s;
+    if (num_node) *num_node = (long)(s + 1) * (s + 1) * (s + 1);
+    return LULESH_OK;
+}
+
+int lulesh_mesh_build(int s, int init_mode, lulesh_mesh_view *out)
+{
+    if (!out || s < 1 || s > lulesh::kMaxEdge) return LULESH_ERR_ARG;
+    if (init_mode != LULESH_INIT_V1 && init_mode != LULESH_INIT_V2) return LULESH_ERR_ARG;
+    lulesh::HostMesh m;
+    m.build(s, init_mode);
+    auto put_d = [](double *dst, const std::vector<double> &src) {
+        if (dst) std::memcpy(dst, src.data(), src.size() * sizeof(double));
+    };
+    auto put_i = [](int *dst, const std::vector<int> &src) {
+        if (dst) std::memcpy(dst, src.data(), src.size() * sizeof(int));
+    };
+    put_d(out->x, m.x);
+    put_d(out->y, m.y);
+    put_d(out->z, m.z);
+    put_d(out->volo, m.volo);
+    put_d(out->elem_mass, m.elem_mass);
+    put_d(out->nodal_mass, m.nodal_mass);
+    put_i(out->nodelist, m.nodelist);
+    put_i(out->node_elem_start, m.node_elem_start);
+    put_i(out->node_elem_count, m.node_elem_count);
+    put_i(out->node_elem_corner_list, m.node_elem_corner_list);
+    put_i(out->lxim, m.lxim);
+    put_i(out->lxip, m.lxip);
+    put_i(out->letam, m.letam);
+    put_i(out->letap, m.letap);
+    put_i(out->lzetam, m.lzetam);
+    put_i(out->lzetap, m.lzetap);
+    put_i(out->elem_bc, m.elem_bc);
+    out->e0 = m.e0;
+    out->dt0 = m.dt0;
+    return LULESH_OK;
+}
+
+}  // extern "C"
