@@ -151,7 +151,7 @@ def config_for(args, ne, nn) -> dict:
             "elements": ne, "nodes": nn, "init": "LULESH 2.0 (e0=3.948746e7*(s/45)^3)",
             "cycles_per_step": 1, "precision": args.precision,
             "l2": "no flush: the state (~4.5 GB) is far larger than the 129 MB L2",
-            "parallelism": "replicas" if args.gpus > 1 else "single"}
+            "parallelism": "replicas" if args.gpus > 1 else "single", "launch": args.launch}
 
 
 def run_reference(args, world, rank):
@@ -183,6 +183,9 @@ def main():
     ap.add_argument("--e2e-cycles", type=int, default=0, help="0: same as --steps")
     ap.add_argument("--cpu-cycles", type=int, default=8, help="cycles of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--launch", default="graph", choices=["graph", "direct"],
+                    help="graph: the captured run loop (product path); direct: the same kernels "
+                         "launched one by one (used for ncu captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -221,13 +224,14 @@ def main():
         return float(t.item())
 
     # ---- warm-up, then K cycles through the run-loop graph ----------------
-    assert g.run(args.warmup) == args.warmup
+    run = g.run if args.launch == "graph" else (lambda n: g.run_profiled(n)[0])
+    assert run(args.warmup) == args.warmup
     launches0 = g.kernel_launches
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         ev0.record(stream)
-        done = g.run(args.steps)
+        done = run(args.steps)
         ev1.record(stream)
         barrier()
     ms = max_over_ranks(ev0.elapsed_time(ev1))

@@ -56,10 +56,13 @@ def load_phases(s, cyc):
     return stages
 
 
-def rel_err(a, b):
-    """max |a-b| / max |b| (0 when both are zero)."""
+def rel_err(a, b, scale=0.0):
+    """max |a-b| / max(max |b|, scale) (0 when both are zero).
+
+    ``scale`` is the natural magnitude of a field that is a difference of
+    larger quantities (delv = vnew - v is compared on the scale of vnew)."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
-    scale = np.max(np.abs(b)) if b.size else 0.0
+    scale = max(np.max(np.abs(b)) if b.size else 0.0, scale)
     d = np.max(np.abs(a - b)) if b.size else 0.0
     return 0.0 if d == 0.0 else d / max(scale, 1e-300)
