@@ -188,6 +188,42 @@ int lulesh_run_profiled(lulesh_ctx *ctx, int max_cycles, int *cycles_done, doubl
  * TFLOP/s (2 flops per FMA), from a register-only kernel. */
 int lulesh_probe_fp64_peak(double *tflops);
 
+/* ---- LagrangeNodal without allocation ---------------------------------
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate GPU memory themselves -- code whose device memory is handed out by
+ * a host framework's own pool or arena, or that must not call the allocator
+ * while its work is in flight.  Everything else in this header allocates
+ * inside lulesh_create; this call allocates nothing.
+ *
+ * It performs LagrangeNodal (LULESH-OMP.cc:1685-1704) -- the same kernels as
+ * lulesh_lagrange_nodal -- on arrays the caller owns, all DEVICE pointers in
+ * the reference's layout: nodelist [8E]; node_elem_start, node_elem_count [N]
+ * and node_elem_corner_list [8E] (entries 8*elem+corner,
+ * AllocateNodeElemIndexes :209-268); symm_x/y/z [num_symm] (the symmetry
+ * node sets, :3114-3125); volo, elem_mass, p, q, v, ss [E]; nodal_mass [N].
+ * x, y, z, xd, yd, zd [N] are read and updated in place; fx, fy, fz [N]
+ * receive the nodal forces when all three are non-NULL.  deltatime is the
+ * step's time increment; params supplies u_cut and hgcoef.  stream is a
+ * cudaStream_t (NULL: the default stream); the call returns after that stream
+ * has drained, with LULESH_OK, LULESH_VOLUME_ERROR, or LULESH_ERR_ARG
+ * (message on stderr) for a mesh over the limit or an index out of range.
+ *
+ * Its working memory (per-corner forces, node-to-corner slots, the
+ * symmetry-plane mask, error words) is one fixed device array compiled into
+ * the library: at most 65,536 elements and 131,072 nodes, 26.6 MiB that every
+ * GPU on which this call is used keeps until the process exits.  All calls
+ * share that array, so calls that overlap on the GPU race; order them on one
+ * stream.  The first call on a device looks up the array's address with that
+ * device current; make it before any stream capture begins. */
+int lulesh_lagrange_nodal_noalloc(
+    int num_elem, int num_node, double deltatime, const lulesh_params *params,
+    const int *nodelist, const int *node_elem_start, const int *node_elem_count,
+    const int *node_elem_corner_list, const int *symm_x, const int *symm_y, const int *symm_z,
+    int num_symm, const double *volo, const double *elem_mass, const double *nodal_mass,
+    const double *p, const double *q, const double *v, const double *ss,
+    double *x, double *y, double *z, double *xd, double *yd, double *zd,
+    double *fx, double *fy, double *fz, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
