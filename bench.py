@@ -44,9 +44,26 @@ UNIT = "Mzone-cycles/s"
 KERNELS = ("time_increment", "elem_force", "node_update", "elem_kinematics", "elem_material", "finalize")
 
 
-def algorithmic_bytes(ne: int, nn: int) -> dict:
-    """Compulsory DRAM bytes per launch of each kernel of the plain FP64 path
-    (8-byte doubles, 4-byte indices, every array touched once)."""
+def algorithmic_bytes(ne: int, nn: int, precision: str = "fp64") -> dict:
+    """Compulsory DRAM bytes per launch of each kernel (8-byte doubles,
+    4-byte floats and indices, every array touched once)."""
+    if precision == "split":
+        return {
+            "time_increment": 0,
+            # hi/lo float pairs of x..zd gathered (48/node), nodelist (32),
+            # p q v volo ss mass (48) in; FP32 corner forces (3 x 8 floats) out
+            "elem_force": 48 * nn + (32 + 48 + 96) * ne,
+            # slots (32/elem) + start (4/node), FP32 corner forces (96/elem),
+            # 1/mass (8) + bc (1), x..zd read and written (96), hi/lo pairs out (48)
+            "node_update": (4 + 8 + 1 + 96 + 48) * nn + (32 + 96) * ne,
+            # nodelist, FP64 x..zd and their hi/lo pairs gathered, volo, v in;
+            # vnew delv vdov arealg (FP64) and six FP32 Q gradients out
+            "elem_kinematics": 96 * nn + (32 + 16 + 32 + 24) * ne,
+            # bc + neighbour ids, FP32 gradients, vnew vdov delv arealg volo mass
+            # q v e p in; p e q ss v out
+            "elem_material": (4 + 24 + 24 + 80 + 40) * ne,
+            "finalize": 0,
+        }
     return {
         "time_increment": 0,
         # x,y,z,xd,yd,zd gathered (48/node), nodelist (32), p q v volo ss mass
@@ -183,6 +200,7 @@ def main():
     ap.add_argument("--e2e-cycles", type=int, default=0, help="0: same as --steps")
     ap.add_argument("--cpu-cycles", type=int, default=8, help="cycles of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-split", action="store_true", help="skip the split-precision leg")
     ap.add_argument("--launch", default="graph", choices=["graph", "direct"],
                     help="graph: the captured run loop (product path); direct: the same kernels "
                          "launched one by one (used for ncu captures)")
@@ -208,7 +226,6 @@ def main():
 
     g = pkg.Lulesh(args.size, pkg.INIT_V2, precision)
     ne, nn = g.num_elem, g.num_node
-    stream = torch.cuda.ExternalStream(g.stream)
 
     def barrier():
         torch.cuda.synchronize()
@@ -223,45 +240,59 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         return float(t.item())
 
-    # ---- warm-up, then K cycles through the run-loop graph ----------------
-    run = g.run if args.launch == "graph" else (lambda n: g.run_profiled(n)[0])
-    assert run(args.warmup) == args.warmup
-    launches0 = g.kernel_launches
-    barrier()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
-        ev0.record(stream)
-        done = run(args.steps)
-        ev1.record(stream)
+    def timed(ctx, steps, clocks=None):
+        """K cycles after W warm-up cycles; device ms on the library's stream."""
+        run = ctx.run if args.launch == "graph" else (lambda n: ctx.run_profiled(n)[0])
+        assert run(args.warmup) == args.warmup
+        st = torch.cuda.ExternalStream(ctx.stream)
+        l0 = ctx.kernel_launches
         barrier()
-    ms = max_over_ranks(ev0.elapsed_time(ev1))
-    launches = g.kernel_launches - launches0
-    assert done == args.steps, (done, args.steps)
-    value = world * ne * args.steps / (ms * 1e-3) * 1e-6
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if clocks is not None:
+            clocks.__enter__()
+        e0.record(st)
+        done = run(steps)
+        e1.record(st)
+        barrier()
+        if clocks is not None:
+            clocks.__exit__(None, None, None)
+        assert done == steps, (done, steps)
+        return max_over_ranks(e0.elapsed_time(e1)), ctx.kernel_launches - l0
 
-    # ---- per-kernel device times (kernel-by-kernel pass) ------------------
-    pc, kms = g.run_profiled(args.profile_cycles)
-    per_launch_ms = {k: v / max(pc, 1) for k, v in kms.items()}
-    abytes = algorithmic_bytes(ne, nn)
-    peaks = measured_peaks()
-    top = max(("elem_force", "node_update", "elem_kinematics", "elem_material"), key=lambda k: per_launch_ms[k])
-    achieved = abytes[top] / (per_launch_ms[top] * 1e-3) * 1e-9
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        t = json.loads(tf.read_text()).get(args.precision, {}).get(top)
-        if t:
-            traffic = t["bytes_per_elem"] * ne
-    roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+    def kernel_table(ctx, precision):
+        """Per-kernel device time from a kernel-by-kernel pass, the roofline
+        of the dominant kernel, and the algorithmic bytes per zone-cycle."""
+        pc, kms = ctx.run_profiled(args.profile_cycles)
+        per_launch = {k: v / max(pc, 1) for k, v in kms.items()}
+        abytes = algorithmic_bytes(ne, nn, precision)
+        peaks = measured_peaks()
+        top = max(("elem_force", "node_update", "elem_kinematics", "elem_material"), key=lambda k: per_launch[k])
+        achieved = abytes[top] / (per_launch[top] * 1e-3) * 1e-9
+        traffic = None
+        tf = ROOT / "profiles" / "traffic.json"
+        if tf.exists():
+            t = json.loads(tf.read_text()).get(precision, {}).get(top)
+            if t:
+                traffic = t["bytes_per_elem"] * ne
+        roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                 "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": abytes[top]}
-    cycle_bytes = sum(abytes.values())
-    total_ms = sum(per_launch_ms.values())
+        total = sum(per_launch.values())
+        table = {k: {"ms": per_launch[k], "share": per_launch[k] / total,
+                     "gbs": abytes[k] / (per_launch[k] * 1e-3) * 1e-9 if per_launch[k] > 0 else 0.0}
+                 for k in KERNELS}
+        return roof, table, sum(abytes.values()) / ne
+
+    mesh = pkg.mesh_build(args.size, pkg.INIT_V2)
+
+    # ---- plain FP64: K cycles through the run-loop graph -----------------
+    clocks = ClockSampler(local)
+    ms, launches = timed(g, args.steps, clocks)
+    value = world * ne * args.steps / (ms * 1e-3) * 1e-6
+    ref_metrics = pkg.sedov_metrics(g, mesh)          # state after W + K cycles
+    roofline, kernels, cycle_bytes = kernel_table(g, args.precision)
     fp64_peak = pkg.probe_fp64_peak()
-    kernels = {k: {"ms": per_launch_ms[k], "share": per_launch_ms[k] / total_ms,
-                   "gbs": abytes[k] / (per_launch_ms[k] * 1e-3) * 1e-9 if per_launch_ms[k] > 0 else 0.0}
-               for k in KERNELS}
 
     # ---- end to end through the C ABI with host buffers -------------------
     e2e_cycles = args.e2e_cycles or args.steps
@@ -284,8 +315,24 @@ def main():
            "h2d_bytes_per_step": state_bytes / e2e_cycles,
            "d2h_bytes_per_step": (state_bytes + 2 * scalar_bytes * e2e_cycles) / e2e_cycles,
            "timer": "host wall clock around upload + per-cycle ABI calls + download"}
-    origin_e = g.origin_energy()
+    del host
     g.close()
+
+    # ---- split precision on the same workload (config 2) ------------------
+    split = None
+    if args.precision == "fp64" and not args.no_split:
+        gs = pkg.Lulesh(args.size, pkg.INIT_V2, pkg.SPLIT)
+        sms, slaunch = timed(gs, args.steps)
+        svalue = world * ne * args.steps / (sms * 1e-3) * 1e-6
+        smetrics = pkg.sedov_metrics(gs, mesh)
+        sroof, skernels, sbytes = kernel_table(gs, "split")
+        gs.close()
+        split = {"value": svalue, "unit": UNIT, "ms_per_step": sms / args.steps,
+                 "speedup_vs_fp64": svalue / value, "gpu_launches": slaunch,
+                 "errors_vs_fp64": pkg.relative_errors(smetrics, ref_metrics),
+                 "compared_at_cycle": args.warmup + args.steps, "results": smetrics,
+                 "roofline": sroof, "kernels": skernels, "bytes_per_zone_cycle": sbytes,
+                 "dtype": "f32 geometry/forces/Q, f64 state/EOS/volume/vdov/dt"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -299,9 +346,9 @@ def main():
                 "config": config_for(args, ne, nn), "roofline": roofline,
                 "fp64": {"peak_tflops_probe": fp64_peak,
                          "note": "the FP64 pipe, not HBM, bounds this path: see kernels[*].gbs"},
-                "bytes_per_zone_cycle": cycle_bytes / ne,
+                "bytes_per_zone_cycle": cycle_bytes,
                 "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clocks.summary(), "origin_energy_after": origin_e}
+                "clocks": clocks.summary(), "results": ref_metrics, "split": split}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

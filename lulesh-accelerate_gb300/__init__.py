@@ -31,7 +31,7 @@ import numpy as np
 __all__ = [
     "Parameters", "Domain", "Scalars", "Lulesh", "lulesh", "library_path", "load_library",
     "LuleshError", "VolumeError", "QStopError", "mesh_build", "mesh_sizes", "default_parameters",
-    "INIT_V1", "INIT_V2", "FP64", "SPLIT",
+    "INIT_V1", "INIT_V2", "FP64", "SPLIT", "sedov_metrics", "relative_errors", "probe_fp64_peak",
 ]
 
 _PKG = Path(__file__).resolve().parent
@@ -362,6 +362,41 @@ class Lulesh:
     @property
     def kernel_launches(self) -> int:
         return load_library().lulesh_kernel_launches(self._h)
+
+
+def sedov_metrics(ctx: "Lulesh", mesh: dict | None = None) -> dict:
+    """Whole-problem results of a Sedov state, for comparing precisions.
+
+    * ``origin_energy``: e of element 0 (the reference's printed result);
+    * ``total_energy``: internal plus kinetic energy,
+      sum(e * elemMass) + sum(0.5 * nodalMass * |v|^2);
+    * ``max_velocity``: largest nodal speed |v|;
+    * ``shock_radius``: artificial-viscosity-weighted mean radius of the
+      element centroids, sum(r q m) / sum(q m).  The monotonic q is non-zero
+      only in the compression zone, so this follows the shock front and,
+      unlike "radius of the element of largest pressure", varies smoothly.
+      The reference defines no shock radius; this is this library's
+      definition.
+    """
+    m = mesh if mesh is not None else mesh_build(ctx.s, INIT_V2)
+    x, y, z = (ctx.get_field(k) for k in ("x", "y", "z"))
+    xd, yd, zd = (ctx.get_field(k) for k in ("xd", "yd", "zd"))
+    e, q = ctx.get_field("e"), ctx.get_field("q")
+    speed2 = xd * xd + yd * yd + zd * zd
+    nl = m["nodelist"].reshape(-1, 8)
+    cx, cy, cz = x[nl].mean(axis=1), y[nl].mean(axis=1), z[nl].mean(axis=1)
+    r = np.sqrt(cx * cx + cy * cy + cz * cz)
+    w = q * m["elem_mass"]
+    return {
+        "origin_energy": float(e[0]),
+        "total_energy": float(np.sum(e * m["elem_mass"]) + 0.5 * np.sum(m["nodal_mass"] * speed2)),
+        "max_velocity": float(np.sqrt(np.max(speed2))),
+        "shock_radius": float(np.sum(r * w) / np.sum(w)) if np.sum(w) > 0 else 0.0,
+    }
+
+
+def relative_errors(got: dict, ref: dict) -> dict:
+    return {k: abs(got[k] - ref[k]) / abs(ref[k]) if ref[k] else abs(got[k]) for k in ref}
 
 
 def probe_fp64_peak() -> float:

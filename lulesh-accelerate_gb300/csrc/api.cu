@@ -167,6 +167,38 @@ int download(lulesh_ctx *ctx, double *dst, const double *src, long n)
     return LULESH_OK;
 }
 
+bool is_split(const lulesh_ctx *ctx) { return ctx->precision == LULESH_PRECISION_SPLIT; }
+
+// After the host replaced FP64 node state, refresh the split path's hi/lo
+// copies (a no-op for the FP64 path).
+int refresh_split(lulesh_ctx *ctx)
+{
+    if (!is_split(ctx)) return LULESH_OK;
+    launch_split_sync(ctx->dom, ctx->stream);
+    int rc = check_launch(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return LULESH_OK;
+}
+
+void nodal(lulesh_ctx *ctx, const Dom &d)
+{
+    if (is_split(ctx)) launch_lagrange_nodal_split(d, ctx->stream);
+    else launch_lagrange_nodal(d, ctx->stream);
+}
+
+void elements(lulesh_ctx *ctx, const Dom &d, bool with_constraints)
+{
+    if (is_split(ctx)) launch_lagrange_elements_split(d, ctx->stream, with_constraints);
+    else launch_lagrange_elements(d, ctx->stream, with_constraints);
+}
+
+void run_body(lulesh_ctx *ctx, const Dom &d, cudaGraphConditionalHandle h)
+{
+    if (is_split(ctx)) launch_run_body_split(d, ctx->stream, h, ctx->d_active);
+    else launch_run_body(d, ctx->stream, h, ctx->d_active);
+}
+
 // Build the run-loop graph: prologue -> while(cond) { one cycle }.  Falls
 // back to a host-driven graph of kChunkCycles gated cycles when conditional
 // nodes are not available.
@@ -202,7 +234,7 @@ int build_run_graph(lulesh_ctx *ctx)
             if (ok) {
                 Dom d = ctx->dom;
                 d.gate = nullptr;
-                launch_run_body(d, ctx->stream, h, ctx->d_active);
+                run_body(ctx, d, h);
                 cudaGraph_t out = nullptr;
                 ok = cudaStreamEndCapture(ctx->stream, &out) == cudaSuccess;
             }
@@ -228,7 +260,7 @@ int build_run_graph(lulesh_ctx *ctx)
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     Dom d = ctx->dom;
     d.gate = ctx->d_active;
-    for (int i = 0; i < kChunkCycles; ++i) launch_run_body(d, ctx->stream, 0, ctx->d_active);
+    for (int i = 0; i < kChunkCycles; ++i) run_body(ctx, d, 0);
     CK(cudaStreamEndCapture(ctx->stream, &cg));
     cudaError_t e = cudaGraphInstantiate(&ctx->chunk_exec, cg, 0);
     cudaGraphDestroy(cg);
@@ -311,8 +343,14 @@ int lulesh_create(int s, int init_mode, int precision, const lulesh_params *para
     A(d.vnew, ne); A(d.delv, ne); A(d.vdov, ne); A(d.arealg, ne); A(d.ql, ne); A(d.qq, ne);
     A(d.delv_xi, ne); A(d.delv_eta, ne); A(d.delv_zeta, ne);
     A(d.delx_xi, ne); A(d.delx_eta, ne); A(d.delx_zeta, ne);
-    A(d.fsx, 8 * ne); A(d.fsy, 8 * ne); A(d.fsz, 8 * ne);
-    A(d.fhx, 8 * ne); A(d.fhy, 8 * ne); A(d.fhz, 8 * ne);
+    if (precision == LULESH_PRECISION_FP64) {
+        A(d.fsx, 8 * ne); A(d.fsy, 8 * ne); A(d.fsz, 8 * ne);
+        A(d.fhx, 8 * ne); A(d.fhy, 8 * ne); A(d.fhz, 8 * ne);
+    } else {
+        A(d.f32x, 8 * ne); A(d.f32y, 8 * ne); A(d.f32z, 8 * ne);
+        A(d.xs, nn); A(d.ys, nn); A(d.zs, nn); A(d.xds, nn); A(d.yds, nn); A(d.zds, nn);
+        A(d.inv_mass, nn); A(d.gq, 6 * ne);
+    }
     A(d.sc, 1); A(ctx->d_active, 1); A(ctx->d_max_cycles, 1);
 #undef A
     d.nodelist = nodelist;
@@ -366,7 +404,12 @@ int lulesh_create(int s, int init_mode, int precision, const lulesh_params *para
     h->cycle = 0;
     h->courant_key = ~0ULL;
     h->hydro_key = ~0ULL;
-    ok = ok && up(d.sc, h, sizeof *h) && cudaStreamSynchronize(st) == cudaSuccess;
+    ok = ok && up(d.sc, h, sizeof *h);
+    if (ok && precision == LULESH_PRECISION_SPLIT) {
+        launch_split_sync(d, st);
+        ok = cudaGetLastError() == cudaSuccess;
+    }
+    ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
     if (!ok) {
         ctx->err = std::string("lulesh_create upload: ") + cudaGetErrorString(cudaGetLastError());
         return bail(LULESH_ERR_CUDA);
@@ -439,7 +482,7 @@ int lulesh_upload_domain(lulesh_ctx *ctx, const double *x, const double *y, cons
     CK(cudaMemcpyAsync(d.sc, ctx->h_sc, sizeof(DevScalars), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->status = LULESH_OK;
-    return LULESH_OK;
+    return refresh_split(ctx);
 }
 
 int lulesh_download_domain(lulesh_ctx *ctx, double *x, double *y, double *z, double *xd, double *yd,
@@ -504,6 +547,19 @@ int lulesh_get_field(lulesh_ctx *ctx, const char *name, double *host, long n)
     double *f = find_field(ctx, name, &node, &writable);
     if (!f) return fail(ctx, LULESH_ERR_ARG, std::string("unknown field ") + name);
     if (n != (node ? ctx->nn : ctx->ne)) return fail(ctx, LULESH_ERR_ARG, std::string("wrong length for field ") + name);
+    if (is_split(ctx)) {
+        // the split path keeps the monotonic-Q gradients in FP32
+        static const char *gnames[6] = {"delv_xi", "delv_eta", "delv_zeta", "delx_xi", "delx_eta", "delx_zeta"};
+        for (int g = 0; g < 6; ++g)
+            if (!strcmp(name, gnames[g])) {
+                std::vector<float> tmp((size_t)n);
+                CK(cudaMemcpyAsync(tmp.data(), ctx->dom.gq + (size_t)g * ctx->ne, n * sizeof(float),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+                CK(cudaStreamSynchronize(ctx->stream));
+                for (long i = 0; i < n; ++i) host[i] = tmp[(size_t)i];
+                return LULESH_OK;
+            }
+    }
     CK(cudaMemcpyAsync(host, f, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return LULESH_OK;
@@ -518,7 +574,8 @@ int lulesh_set_field(lulesh_ctx *ctx, const char *name, const double *host, long
     if (n != (node ? ctx->nn : ctx->ne)) return fail(ctx, LULESH_ERR_ARG, std::string("wrong length for field ") + name);
     CK(cudaMemcpyAsync(f, host, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    return clear_errors(ctx);
+    int rc = clear_errors(ctx);
+    return rc ? rc : refresh_split(ctx);
 }
 
 int lulesh_time_increment(lulesh_ctx *ctx)
@@ -535,7 +592,7 @@ int lulesh_lagrange_nodal(lulesh_ctx *ctx)
 {
     if (!ctx) return LULESH_ERR_ARG;
     if (ctx->status) return ctx->status;
-    launch_lagrange_nodal(ctx->dom, ctx->stream);
+    nodal(ctx, ctx->dom);
     ctx->launches += 2;
     int rc = check_launch(ctx);
     return rc ? rc : read_status(ctx);
@@ -545,7 +602,7 @@ int lulesh_lagrange_elements(lulesh_ctx *ctx)
 {
     if (!ctx) return LULESH_ERR_ARG;
     if (ctx->status) return ctx->status;
-    launch_lagrange_elements(ctx->dom, ctx->stream, false);
+    elements(ctx, ctx->dom, false);
     ctx->launches += 2;
     int rc = check_launch(ctx);
     return rc ? rc : read_status(ctx);
@@ -565,8 +622,8 @@ int lulesh_lagrange_leapfrog(lulesh_ctx *ctx)
 {
     if (!ctx) return LULESH_ERR_ARG;
     if (ctx->status) return ctx->status;
-    launch_lagrange_nodal(ctx->dom, ctx->stream);
-    launch_lagrange_elements(ctx->dom, ctx->stream, true);
+    nodal(ctx, ctx->dom);
+    elements(ctx, ctx->dom, true);
     launch_finalize(ctx->dom, ctx->stream);
     ctx->launches += 5;
     int rc = check_launch(ctx);
@@ -618,7 +675,8 @@ int lulesh_run_profiled(lulesh_ctx *ctx, int max_cycles, int *cycles_done, doubl
         if ((rc = read_status(ctx))) break;
         const DevScalars *h = ctx->h_sc;
         if (!(h->time < d.prm.stoptime) || !(h->deltatime > 0.0) || done >= cap) break;
-        launch_cycle_timed(d, ctx->stream, ev);
+        if (is_split(ctx)) launch_cycle_timed_split(d, ctx->stream, ev);
+        else launch_cycle_timed(d, ctx->stream, ev);
         if ((rc = check_launch(ctx))) break;
         CK(cudaEventSynchronize(ev[kTimedKernels]));
         for (int i = 0; i < kTimedKernels && kernel_ms; ++i) {

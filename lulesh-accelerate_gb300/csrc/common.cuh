@@ -1,0 +1,284 @@
+// common.cuh -- device helpers shared by the FP64 and split-precision steps.
+#pragma once
+
+#include "lulesh_internal.h"
+
+#include <cuda_runtime.h>
+
+namespace lulesh {
+
+__device__ __forceinline__ void load_nodelist(const int *nodelist, int k, int nl[8])
+{
+    const int4 *p = reinterpret_cast<const int4 *>(nodelist + 8 * (size_t)k);
+    const int4 a = __ldg(p), b = __ldg(p + 1);
+    nl[0] = a.x; nl[1] = a.y; nl[2] = a.z; nl[3] = a.w;
+    nl[4] = b.x; nl[5] = b.y; nl[6] = b.z; nl[7] = b.w;
+}
+
+__device__ __forceinline__ void gather8(const double *__restrict__ f, const int nl[8], double out[8])
+{
+#pragma unroll
+    for (int c = 0; c < 8; ++c) out[c] = __ldg(f + nl[c]);
+}
+
+__device__ __forceinline__ void flag_error(DevScalars *sc, int site, int elem)
+{
+    sc->err[site] = elem + 1;
+    sc->err_any = 1;
+}
+
+// A kernel of the step does nothing once an earlier phase of the cycle has
+// flagged an error (the reference would have exited), or when the run loop
+// has been stopped (only in the host-driven fallback loop, where d.gate is
+// set).  Kernels that use a block barrier evaluate this into a flag instead
+// of returning, so that every thread reaches the barrier.
+__device__ __forceinline__ bool skip_step(const Dom &d)
+{
+    return d.sc->err_any != 0 || (d.gate != nullptr && *d.gate == 0);
+}
+
+// ---------------------------------------------------------------------
+// TimeIncrement (LULESH-OMP.cc:557-604)
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void time_increment(DevScalars *sc, const lulesh_params &P)
+{
+    double targetdt = P.stoptime - sc->time;
+    if ((P.dtfixed <= 0.0) && (sc->cycle != 0)) {
+        const double olddt = sc->deltatime;
+        double newdt = 1.0e+20;
+        if (sc->dtcourant < newdt) newdt = sc->dtcourant / 2.0;
+        if (sc->dthydro < newdt) newdt = sc->dthydro * 2.0 / 3.0;
+        const double ratio = newdt / olddt;
+        if (ratio >= 1.0) {
+            if (ratio < P.deltatimemultlb) newdt = olddt;
+            else if (ratio > P.deltatimemultub) newdt = olddt * P.deltatimemultub;
+        }
+        if (newdt > P.dtmax) newdt = P.dtmax;
+        sc->deltatime = newdt;
+    }
+    if ((targetdt > sc->deltatime) && (targetdt < (4.0 * sc->deltatime / 3.0)))
+        targetdt = 2.0 * sc->deltatime / 3.0;
+    if (targetdt < sc->deltatime) sc->deltatime = targetdt;
+    sc->time += sc->deltatime;
+    ++sc->cycle;
+}
+
+// One direction of the monotonic limiter (:2198-2228).
+template <typename T>
+__device__ __forceinline__ T limiter_phi(const T *__restrict__ delv, int i, int bm, int bp,
+                                         int m_symm, int m_free, int p_symm, int p_free,
+                                         int lm, int lp, T limiter, T max_slope)
+{
+    const T ptiny = T(1.e-36);
+    const T own = delv[i];
+    const T norm = T(1.) / (own + ptiny);
+    T delvm = T(0.0), delvp = T(0.0);
+    if (bm == 0) delvm = delv[lm];
+    else if (bm == m_symm) delvm = own;
+    else if (bm == m_free) delvm = 0.0;
+    if (bp == 0) delvp = delv[lp];
+    else if (bp == p_symm) delvp = own;
+    else if (bp == p_free) delvp = 0.0;
+    delvm = delvm * norm;
+    delvp = delvp * norm;
+    T phi = T(.5) * (delvm + delvp);
+    delvm *= limiter;
+    delvp *= limiter;
+    if (delvm < phi) phi = delvm;
+    if (delvp < phi) phi = delvp;
+    if (phi < T(0.)) phi = T(0.);
+    if (phi > max_slope) phi = max_slope;
+    return phi;
+}
+
+// CalcPressureForElems for one element (:2384-2413).
+__device__ __forceinline__ double eos_pressure(double &bvc, double e, double comp, double vnewc,
+                                               const lulesh_params &P)
+{
+    const double c1s = 2.0 / 3.0;
+    bvc = c1s * (comp + 1.);
+    double p = bvc * e;
+    if (fabs(p) < P.p_cut) p = 0.0;
+    if (vnewc >= P.eosvmax) p = 0.0;
+    if (p < P.pmin) p = P.pmin;
+    return p;
+}
+
+// sqrt((pbvc*e + vv^2*bvc*p)/rho0) with the reference's floor (:2485-2493).
+__device__ __forceinline__ double sound_term(double pbvc, double e, double vv, double bvc, double p,
+                                             double rho0, bool unit_rho0)
+{
+    double ssc = pbvc * e + vv * vv * bvc * p;
+    if (!unit_rho0) ssc = ssc / rho0;   // x / 1.0 == x: the division is skipped only then
+    if (ssc <= .111111e-36) ssc = .333333e-18;
+    else ssc = sqrt(ssc);
+    return ssc;
+}
+
+// The qstop test, ApplyMaterialPropertiesForElems, EvalEOSForElems +
+// CalcEnergyForElems + CalcSoundSpeedForElems and UpdateVolumesForElems for
+// element k (LULESH-OMP.cc:2369-2381, :2384-2782), given its monotonic-Q
+// terms; every loop of the reference there is element-local.  Writes
+// p, e, q, ss and v and returns the new sound speed.
+__device__ __forceinline__ double material_update(const Dom &d, int k, DevScalars *sc, double vnew,
+                                                  double qlin, double qquad)
+{
+    const lulesh_params &P = d.prm;
+    // CalcQForElems qstop test on the old q (:2369-2381)
+    const double q_old = d.q[k];
+    if (q_old > P.qstop) flag_error(sc, ERR_K3_QSTOP, k);
+
+    // ApplyMaterialPropertiesForElems (:2703-2761)
+    const double eosvmin = P.eosvmin, eosvmax = P.eosvmax;
+    double vnewc = vnew;
+    if (eosvmin != 0. && vnewc < eosvmin) vnewc = eosvmin;
+    if (eosvmax != 0. && vnewc > eosvmax) vnewc = eosvmax;
+    const double v_old = d.v[k];
+    double vc = v_old;
+    if (eosvmin != 0. && vc < eosvmin) vc = eosvmin;
+    if (eosvmax != 0. && vc > eosvmax) vc = eosvmax;
+    if (vc <= 0.) flag_error(sc, ERR_K3_MATV, k);
+
+    // EvalEOSForElems + CalcEnergyForElems (:2415-2701); work == 0
+    const double delvc = d.delv[k], e_old = d.e[k];
+    double p_old = d.p[k];
+    double compression = 1. / vnewc - 1.;
+    const double vchalf = vnewc - delvc * .5;
+    double comp_half = 1. / vchalf - 1.;
+    if (eosvmin != 0. && vnewc <= eosvmin) comp_half = compression;
+    if (eosvmax != 0. && vnewc >= eosvmax) {
+        p_old = 0.;
+        compression = 0.;
+        comp_half = 0.;
+    }
+    const double rho0 = P.refdens;
+    const bool unit_rho0 = (rho0 == 1.0);
+    const double pbvc = 2.0 / 3.0;
+    const double emin = P.emin, e_cut = P.e_cut;
+    double bvc;
+
+    double e_new = e_old - .5 * delvc * (p_old + q_old);
+    if (e_new < emin) e_new = emin;
+    const double p_half = eos_pressure(bvc, e_new, comp_half, vnewc, P);
+    const double vhalf = 1. / (1. + comp_half);
+    double q_new = 0.;
+    if (!(delvc > 0.)) q_new = sound_term(pbvc, e_new, vhalf, bvc, p_half, rho0, unit_rho0) * qlin + qquad;
+    e_new = e_new + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (p_half + q_new));
+    if (fabs(e_new) < e_cut) e_new = 0.;
+    if (e_new < emin) e_new = emin;
+
+    double p_new = eos_pressure(bvc, e_new, compression, vnewc, P);
+    double q_tilde = 0.;
+    if (!(delvc > 0.)) q_tilde = sound_term(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0) * qlin + qquad;
+    const double sixth = 1.0 / 6.0;
+    e_new = e_new - (7.0 * (p_old + q_old) - 8.0 * (p_half + q_new) + (p_new + q_tilde)) * delvc * sixth;
+    if (fabs(e_new) < e_cut) e_new = 0.;
+    if (e_new < emin) e_new = emin;
+
+    p_new = eos_pressure(bvc, e_new, compression, vnewc, P);
+    const double ssn = sound_term(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0);
+    if (delvc <= 0.) {
+        q_new = ssn * qlin + qquad;
+        if (fabs(q_new) < P.q_cut) q_new = 0.;
+    }
+    d.p[k] = p_new;
+    d.e[k] = e_new;
+    d.q[k] = q_new;
+    d.ss[k] = ssn;     // CalcSoundSpeedForElems (:2543-2561)
+
+    // UpdateVolumesForElems (:2763-2782)
+    double vt = vnew;
+    if (fabs(vt - 1.0) < P.v_cut) vt = 1.0;
+    d.v[k] = vt;
+    return ssn;
+}
+
+// Order-preserving map of a double onto uint64 (NaN maps to the maximum, so
+// it never wins a minimum, as in the reference's '<' tests).
+__device__ __forceinline__ unsigned long long order_key(double v)
+{
+    if (v != v) return ~0ULL;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b & 0x8000000000000000ULL) ? ~b : (b | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double key_value(unsigned long long k)
+{
+    const unsigned long long b = (k & 0x8000000000000000ULL) ? (k & 0x7fffffffffffffffULL) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+
+// Block-wide minimum of two keys, one atomicMin each per block.
+__device__ __forceinline__ void block_min_publish(unsigned long long kc, unsigned long long kh,
+                                                  DevScalars *sc)
+{
+    __shared__ unsigned long long s_c[32], s_h[32];
+    kc = warp_min_u64(kc);
+    kh = warp_min_u64(kh);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { s_c[warp] = kc; s_h[warp] = kh; }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        kc = lane < nw ? s_c[lane] : ~0ULL;
+        kh = lane < nw ? s_h[lane] : ~0ULL;
+        kc = warp_min_u64(kc);
+        kh = warp_min_u64(kh);
+        if (lane == 0) {
+            if (kc != ~0ULL) atomicMin(&sc->courant_key, kc);
+            if (kh != ~0ULL) atomicMin(&sc->hydro_key, kh);
+        }
+    }
+}
+
+// Constraint candidates of one element (:2820-2855, :2897-2915).
+__device__ __forceinline__ void constraint_keys(double ss, double vdov, double arealg,
+                                                const lulesh_params &P,
+                                                unsigned long long &kc, unsigned long long &kh)
+{
+    kc = ~0ULL;
+    kh = ~0ULL;
+    if (vdov != 0.) {
+        const double qqc2 = 64.0 * P.qqc * P.qqc;
+        double dtf = ss * ss;
+        if (vdov < 0.) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
+        dtf = sqrt(dtf);
+        dtf = arealg / dtf;
+        kc = order_key(dtf);
+        kh = order_key(P.dvovmax / (fabs(vdov) + 1.e-20));
+    }
+}
+
+// Publish the constraint minima: a value is registered only when some
+// element was active and it is below the 1e20 start value (:2869-2871,
+// :2928-2930); otherwise the previous dtcourant/dthydro stay.
+__device__ __forceinline__ void finalize_constraints(DevScalars *sc)
+{
+    const unsigned long long limit = order_key(1.0e+20);
+    if (sc->courant_key < limit) sc->dtcourant = key_value(sc->courant_key);
+    if (sc->hydro_key < limit) sc->dthydro = key_value(sc->hydro_key);
+    sc->courant_key = ~0ULL;
+    sc->hydro_key = ~0ULL;
+}
+
+// Run-loop control: may another cycle start?  Besides the reference's
+// time < stoptime test and the caller's cap, the loop stops when the time
+// step is no longer positive (the reference would spin forever there) and
+// after kRunCycleLimit cycles, so a device-side loop always ends.
+__device__ __forceinline__ unsigned run_continue(const DevScalars *sc, const lulesh_params &P)
+{
+    const int cap = (sc->run_max > 0 && sc->run_max < kRunCycleLimit) ? sc->run_max : kRunCycleLimit;
+    return (sc->err_any == 0) && (sc->time < P.stoptime) && (sc->deltatime > 0.0) &&
+           (sc->run_cycles < cap);
+}
+
+}  // namespace lulesh

@@ -9,13 +9,14 @@ namespace lulesh {
 
 // Jacobian columns of one coordinate at the element centre, scaled by 1/8
 // (LULESH-OMP.cc:650-660).
-__device__ __forceinline__ void jac_column(const double c[8], double &xi, double &et, double &ze)
+template <typename T>
+__device__ __forceinline__ void jac_column(const T c[8], T &xi, T &et, T &ze)
 {
-    const double d60 = c[6] - c[0], d53 = c[5] - c[3];
-    const double d71 = c[7] - c[1], d42 = c[4] - c[2];
-    xi = .125 * (((d60 + d53) - d71) - d42);
-    et = .125 * (((d60 - d53) + d71) - d42);
-    ze = .125 * (((d60 + d53) + d71) + d42);
+    const T d60 = c[6] - c[0], d53 = c[5] - c[3];
+    const T d71 = c[7] - c[1], d42 = c[4] - c[2];
+    xi = T(.125) * (((d60 + d53) - d71) - d42);
+    et = T(.125) * (((d60 - d53) + d71) - d42);
+    ze = T(.125) * (((d60 + d53) + d71) + d42);
 }
 
 // CalcElemShapeFunctionDerivatives (LULESH-OMP.cc:619-706): B for corners
@@ -48,16 +49,17 @@ __device__ __forceinline__ void shape_derivs4(const double x[8], const double y[
 }
 
 // Jacobian volume only (the determinant IntegrateStressForElems checks).
-__device__ __forceinline__ double jacobian_volume(const double x[8], const double y[8], const double z[8])
+template <typename T>
+__device__ __forceinline__ T jacobian_volume(const T x[8], const T y[8], const T z[8])
 {
-    double a[3], t[3], c[3];
+    T a[3], t[3], c[3];
     jac_column(x, a[0], t[0], c[0]);
     jac_column(y, a[1], t[1], c[1]);
     jac_column(z, a[2], t[2], c[2]);
-    const double cet0 = (a[2] * c[1]) - (a[1] * c[2]);
-    const double cet1 = (a[0] * c[2]) - (a[2] * c[0]);
-    const double cet2 = (a[1] * c[0]) - (a[0] * c[1]);
-    return 8.0 * ((t[0] * cet0 + t[1] * cet1) + t[2] * cet2);
+    const T cet0 = (a[2] * c[1]) - (a[1] * c[2]);
+    const T cet1 = (a[0] * c[2]) - (a[2] * c[0]);
+    const T cet2 = (a[1] * c[0]) - (a[0] * c[1]);
+    return T(8.0) * ((t[0] * cet0 + t[1] * cet1) + t[2] * cet2);
 }
 
 // CalcElemNodeNormals + SumElemFaceNormal (LULESH-OMP.cc:708-799).  The six
@@ -102,24 +104,64 @@ __device__ __forceinline__ void node_normals(double pf[3][8], const double x[8],
     }
 }
 
-// VoluDer (LULESH-OMP.cc:978-1006) on six corners given by index.
-__device__ __forceinline__ void volu_der(const double x[8], const double y[8], const double z[8],
-                                         int i0, int i1, int i2, int i3, int i4, int i5,
-                                         double &dx, double &dy, double &dz)
+// Node normals from the face diagonals, for the split-precision step.  For a
+// face (n0,n1,n2,n3) the reference's quarter-area vector
+// 0.25*(b0 x b1), with bisectors b0 = (u+v)/2, b1 = (u-v)/2 of the diagonals
+// u = x[n2]-x[n0], v = x[n3]-x[n1], equals 0.125*(v x u): the same value with
+// 12 operations instead of 27 and no cancellation in the bisector sums.
+template <typename T>
+__device__ __forceinline__ void face_area_diag(const T x[8], const T y[8], const T z[8],
+                                               int n0, int n1, int n2, int n3, T &ax, T &ay, T &az)
 {
-    const double twelfth = 1.0 / 12.0;
-    const double x0 = x[i0], x1 = x[i1], x2 = x[i2], x3 = x[i3], x4 = x[i4], x5 = x[i5];
-    const double y0 = y[i0], y1 = y[i1], y2 = y[i2], y3 = y[i3], y4 = y[i4], y5 = y[i5];
-    const double z0 = z[i0], z1 = z[i1], z2 = z[i2], z3 = z[i3], z4 = z[i4], z5 = z[i5];
-    const double vx =
+    const T ux = x[n2] - x[n0], uy = y[n2] - y[n0], uz = z[n2] - z[n0];
+    const T vx = x[n3] - x[n1], vy = y[n3] - y[n1], vz = z[n3] - z[n1];
+    ax = T(0.125) * (vy * uz - vz * uy);
+    ay = T(0.125) * (vz * ux - vx * uz);
+    az = T(0.125) * (vx * uy - vy * ux);
+}
+
+template <typename T>
+__device__ __forceinline__ void node_normals_diag(T pf[3][8], const T x[8], const T y[8], const T z[8])
+{
+    T a[6][3];
+    face_area_diag(x, y, z, 0, 1, 2, 3, a[0][0], a[0][1], a[0][2]);
+    face_area_diag(x, y, z, 0, 4, 5, 1, a[1][0], a[1][1], a[1][2]);
+    face_area_diag(x, y, z, 1, 5, 6, 2, a[2][0], a[2][1], a[2][2]);
+    face_area_diag(x, y, z, 2, 6, 7, 3, a[3][0], a[3][1], a[3][2]);
+    face_area_diag(x, y, z, 3, 7, 4, 0, a[4][0], a[4][1], a[4][2]);
+    face_area_diag(x, y, z, 4, 7, 6, 5, a[5][0], a[5][1], a[5][2]);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        pf[d][0] = (a[0][d] + a[1][d]) + a[4][d];
+        pf[d][1] = (a[0][d] + a[1][d]) + a[2][d];
+        pf[d][2] = (a[0][d] + a[2][d]) + a[3][d];
+        pf[d][3] = (a[0][d] + a[3][d]) + a[4][d];
+        pf[d][4] = (a[1][d] + a[4][d]) + a[5][d];
+        pf[d][5] = (a[1][d] + a[2][d]) + a[5][d];
+        pf[d][6] = (a[2][d] + a[3][d]) + a[5][d];
+        pf[d][7] = (a[3][d] + a[4][d]) + a[5][d];
+    }
+}
+
+// VoluDer (LULESH-OMP.cc:978-1006) on six corners given by index.
+template <typename T>
+__device__ __forceinline__ void volu_der(const T x[8], const T y[8], const T z[8],
+                                         int i0, int i1, int i2, int i3, int i4, int i5,
+                                         T &dx, T &dy, T &dz)
+{
+    const T twelfth = T(1.0) / T(12.0);
+    const T x0 = x[i0], x1 = x[i1], x2 = x[i2], x3 = x[i3], x4 = x[i4], x5 = x[i5];
+    const T y0 = y[i0], y1 = y[i1], y2 = y[i2], y3 = y[i3], y4 = y[i4], y5 = y[i5];
+    const T z0 = z[i0], z1 = z[i1], z2 = z[i2], z3 = z[i3], z4 = z[i4], z5 = z[i5];
+    const T vx =
         (y1 + y2) * (z0 + z1) - (y0 + y1) * (z1 + z2) +
         (y0 + y4) * (z3 + z4) - (y3 + y4) * (z0 + z4) -
         (y2 + y5) * (z3 + z5) + (y3 + y5) * (z2 + z5);
-    const double vy =
+    const T vy =
         -(x1 + x2) * (z0 + z1) + (x0 + x1) * (z1 + z2) -
         (x0 + x4) * (z3 + z4) + (x3 + x4) * (z0 + z4) +
         (x2 + x5) * (z3 + z5) - (x3 + x5) * (z2 + z5);
-    const double vz =
+    const T vz =
         -(y1 + y2) * (x0 + x1) + (y0 + y1) * (x1 + x2) -
         (y0 + y4) * (x3 + x4) + (y3 + y4) * (x0 + x4) +
         (y2 + y5) * (x3 + x5) - (y3 + y5) * (x2 + x5);
@@ -129,8 +171,9 @@ __device__ __forceinline__ void volu_der(const double x[8], const double y[8], c
 }
 
 // CalcElemVolumeDerivative (LULESH-OMP.cc:1008-1048).
-__device__ __forceinline__ void volume_derivative(double dvdx[8], double dvdy[8], double dvdz[8],
-                                                  const double x[8], const double y[8], const double z[8])
+template <typename T>
+__device__ __forceinline__ void volume_derivative(T dvdx[8], T dvdy[8], T dvdz[8],
+                                                  const T x[8], const T y[8], const T z[8])
 {
     volu_der(x, y, z, 1, 2, 3, 4, 5, 7, dvdx[0], dvdy[0], dvdz[0]);
     volu_der(x, y, z, 0, 1, 2, 7, 4, 6, dvdx[3], dvdy[3], dvdz[3]);
@@ -169,31 +212,31 @@ __device__ __forceinline__ double elem_volume(const double x[8], const double y[
 }
 
 // AreaFace (LULESH-OMP.cc:1799-1819).
-__device__ __forceinline__ double area_face(const double x[8], const double y[8], const double z[8],
-                                            int a, int b, int c, int d)
+template <typename T>
+__device__ __forceinline__ T area_face(const T x[8], const T y[8], const T z[8], int a, int b, int c, int d)
 {
-    const double fx = (x[c] - x[a]) - (x[d] - x[b]);
-    const double fy = (y[c] - y[a]) - (y[d] - y[b]);
-    const double fz = (z[c] - z[a]) - (z[d] - z[b]);
-    const double gx = (x[c] - x[a]) + (x[d] - x[b]);
-    const double gy = (y[c] - y[a]) + (y[d] - y[b]);
-    const double gz = (z[c] - z[a]) + (z[d] - z[b]);
-    const double fg = fx * gx + fy * gy + fz * gz;
+    const T fx = (x[c] - x[a]) - (x[d] - x[b]);
+    const T fy = (y[c] - y[a]) - (y[d] - y[b]);
+    const T fz = (z[c] - z[a]) - (z[d] - z[b]);
+    const T gx = (x[c] - x[a]) + (x[d] - x[b]);
+    const T gy = (y[c] - y[a]) + (y[d] - y[b]);
+    const T gz = (z[c] - z[a]) + (z[d] - z[b]);
+    const T fg = fx * gx + fy * gy + fz * gz;
     return (fx * fx + fy * fy + fz * fz) * (gx * gx + gy * gy + gz * gz) - fg * fg;
 }
 
 // CalcElemCharacteristicLength (LULESH-OMP.cc:1821-1862).
-__device__ __forceinline__ double char_length(const double x[8], const double y[8], const double z[8],
-                                              double volume)
+template <typename T>
+__device__ __forceinline__ T char_length(const T x[8], const T y[8], const T z[8], T volume)
 {
-    double m = 0.0, a;
+    T m = T(0.0), a;
     a = area_face(x, y, z, 0, 1, 2, 3); m = fmax(a, m);
     a = area_face(x, y, z, 4, 5, 6, 7); m = fmax(a, m);
     a = area_face(x, y, z, 0, 1, 5, 4); m = fmax(a, m);
     a = area_face(x, y, z, 1, 2, 6, 5); m = fmax(a, m);
     a = area_face(x, y, z, 2, 3, 7, 6); m = fmax(a, m);
     a = area_face(x, y, z, 3, 0, 4, 7); m = fmax(a, m);
-    return 4.0 * volume / sqrt(m);
+    return T(4.0) * volume / sqrt(m);
 }
 
 }  // namespace lulesh

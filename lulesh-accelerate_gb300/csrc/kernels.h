@@ -22,10 +22,18 @@ void launch_finalize(const Dom &d, cudaStream_t st);
 void launch_run_prologue(const Dom &d, cudaStream_t st, const int *max_cycles,
                          cudaGraphConditionalHandle h, int *active);
 void launch_run_body(const Dom &d, cudaStream_t st, cudaGraphConditionalHandle h, int *active);
+void launch_run_epilogue(const Dom &d, cudaStream_t st, cudaGraphConditionalHandle h, int *active);
 int kernels_per_cycle();
 constexpr int kRunCycleLimit = 1 << 26;
 constexpr int kTimedKernels = 6;   // time increment, force, node, kinematics, material, finalize
 void launch_cycle_timed(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTimedKernels + 1]);
 void launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t st);
+
+// Split-precision path (step_split.cu).
+void launch_split_sync(const Dom &d, cudaStream_t st);
+void launch_lagrange_nodal_split(const Dom &d, cudaStream_t st);
+void launch_lagrange_elements_split(const Dom &d, cudaStream_t st, bool with_constraints);
+void launch_run_body_split(const Dom &d, cudaStream_t st, cudaGraphConditionalHandle h, int *active);
+void launch_cycle_timed_split(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTimedKernels + 1]);
 
 }  // namespace lulesh

@@ -4,6 +4,7 @@
 #include "../../include/lulesh_gb300.h"
 
 #include <cstdint>
+#include <vector_types.h>
 #include <vector>
 
 namespace lulesh {
@@ -82,8 +83,14 @@ struct Dom {
     // corner forces, corner-major [8*ne]: stress and hourglass parts kept
     // apart so that the node sums associate as the reference's do
     double *fsx, *fsy, *fsz, *fhx, *fhy, *fhz;
-    // split-precision corner forces (float, corner-major [8*ne])
+    // split precision: FP32 corner forces (corner-major [8*ne]), hi/lo
+    // float pairs of the FP64 positions and velocities [nn], reciprocal
+    // nodal masses [nn], FP32 monotonic-Q gradients [6][ne] in the order
+    // delv_xi, delv_eta, delv_zeta, delx_xi, delx_eta, delx_zeta
     float *f32x, *f32y, *f32z;
+    float2 *xs, *ys, *zs, *xds, *yds, *zds;
+    double *inv_mass;
+    float *gq;
     DevScalars *sc;
     const int *gate;                     // host-driven run loop: cycle runs while *gate != 0
     lulesh_params prm;

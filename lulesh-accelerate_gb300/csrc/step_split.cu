@@ -1,0 +1,475 @@
+// step_split.cu -- the split-precision Lagrange leapfrog step on sm_103a.
+//
+// GB300 issues FP32 at 64x its FP64 rate, so this step moves the geometry-
+// heavy work to FP32 and keeps FP64 where the solution's stability needs it:
+//
+//   FP32  shape-function geometry, stress and Flanagan-Belytschko hourglass
+//         corner forces (IntegrateStressForElems, CalcFBHourglassForceForElems,
+//         LULESH-OMP.cc:853-931, :1233-1558), the characteristic length and
+//         the monotonic-Q gradients and limiter (:1799-1862, :2034-2320);
+//   FP64  node accelerations, velocities and positions (:1613-1683), the
+//         relative volume and its change, the strain rate vdov (:1927-2032),
+//         CalcEnergyForElems / EOS / sound speed / volume update
+//         (:2384-2782) and the constraint minima (:2799-2933).
+//
+// Corner forces are FP32 and summed per node with a compensated (Kahan)
+// FP32 sum whose two words are combined in FP64.  FP32 geometry never sees an
+// absolute coordinate: every element works on its corners relative to corner
+// 0, formed from a hi/lo float pair that the node kernel keeps beside each
+// FP64 position and velocity ((hi_c - hi_0) + (lo_c - lo_0) carries the
+// difference to ~2^-48 of the coordinate), so FP32 round-off is relative to
+// the element size, not to the mesh extent.
+//
+// Launch structure and error handling are those of step_fp64.cu.
+#include "lulesh_internal.h"
+#include "kernels.h"
+#include "geometry.cuh"
+#include "common.cuh"
+
+#include <cuda_runtime.h>
+
+namespace lulesh {
+
+// Conversions between FP64 and FP32 run on GB300's FP64 pipe at the FP64
+// rate (2 per SM per clock), so this file converts with integer bit
+// operations instead.  Values below FP32's normal range (|v| < 2^-126)
+// become signed zeros; positions, velocities, forces and the element scalars
+// converted here never live there.
+
+// double -> float, mantissa truncated to 23 bits (error < 2^-23 relative).
+__device__ __forceinline__ float d2f(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned hi = (unsigned)(b >> 32);
+    const unsigned sign = hi & 0x80000000u;
+    const int de = (int)((hi >> 20) & 0x7ffu);
+    const unsigned mant = (unsigned)(b >> 29) & 0x7fffffu;
+    if (de == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (mant ? 0x400000u : 0u));   // inf, nan
+    const int fe = de - 1023 + 127;
+    if (fe <= 0) return __uint_as_float(sign);
+    if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned)fe << 23) | mant);
+}
+
+// float -> double, exact (FP32 subnormals become zeros).
+__device__ __forceinline__ double f2d(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned fe = (u >> 23) & 0xffu;
+    const unsigned long long mant = (unsigned long long)(u & 0x7fffffu) << 29;
+    if (fe == 0) return __longlong_as_double((long long)sign);
+    const unsigned long long de = (fe == 0xff) ? 0x7ffULL : (unsigned long long)(fe - 127 + 1023);
+    return __longlong_as_double((long long)(sign | (de << 52) | mant));
+}
+
+// v = hi + lo with hi = v truncated to FP32 precision (exact in FP32) and
+// lo = the remainder (exact in FP64, truncated to FP32): hi + lo carries v to
+// ~2^-46 relative.  One FP64 subtraction, the rest integer operations.
+__device__ __forceinline__ float2 split_hi_lo(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const double hid = __longlong_as_double((long long)(b & ~((1ULL << 29) - 1)));
+    return make_float2(d2f(hid), d2f(v - hid));
+}
+
+// Corner values relative to corner 0, from hi/lo pairs.
+__device__ __forceinline__ void rel8(const float2 *__restrict__ f, const int nl[8], float out[8])
+{
+    const float2 a0 = __ldg(f + nl[0]);
+    out[0] = 0.f;
+#pragma unroll
+    for (int c = 1; c < 8; ++c) {
+        const float2 a = __ldg(f + nl[c]);
+        out[c] = (a.x - a0.x) + (a.y - a0.y);
+    }
+}
+
+// FP64 state -> hi/lo pairs and reciprocal masses (after any host upload).
+__global__ void __launch_bounds__(kBlockNode) k_split_sync(const __grid_constant__ Dom d)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nn) return;
+    d.xs[n] = split_hi_lo(d.x[n]);
+    d.ys[n] = split_hi_lo(d.y[n]);
+    d.zs[n] = split_hi_lo(d.z[n]);
+    d.xds[n] = split_hi_lo(d.xd[n]);
+    d.yds[n] = split_hi_lo(d.yd[n]);
+    d.zds[n] = split_hi_lo(d.zd[n]);
+    d.inv_mass[n] = 1.0 / d.nodal_mass[n];
+}
+
+// ---------------------------------------------------------------------
+// Element force in FP32
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars *sc)
+{
+    const size_t ne = (size_t)d.ne;
+
+    int nl[8];
+    load_nodelist(d.nodelist, k, nl);
+    float x[8], y[8], z[8];
+    rel8(d.xs, nl, x);
+    rel8(d.ys, nl, y);
+    rel8(d.zs, nl, z);
+
+    float f[3][8];
+    {
+        const float determ = jacobian_volume<float>(x, y, z);
+        if (determ <= 0.f) flag_error(sc, ERR_K1_DETERM, k);
+        float pf[3][8];
+        node_normals_diag<float>(pf, x, y, z);
+        const float sig = -d2f(d.p[k]) - d2f(d.q[k]);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            f[0][c] = -(sig * pf[0][c]);
+            f[1][c] = -(sig * pf[1][c]);
+            f[2][c] = -(sig * pf[2][c]);
+        }
+    }
+
+    const double vk = d.v[k];
+    if (vk <= 0.0) flag_error(sc, ERR_K1_VOLUME, k);
+    const float hourg = d2f(d.prm.hgcoef);
+    if (hourg > 0.f) {
+        const float determ = d2f(d.volo[k]) * d2f(vk);
+        float hg[8][4];
+        {
+            float dvdx[8], dvdy[8], dvdz[8];
+            volume_derivative<float>(dvdx, dvdy, dvdz, x, y, z);
+            const float volinv = 1.f / determ;
+#define HMOD(f, s0, s1, s2, s3, s4, s5, s6, s7) \
+            ((((((((s0 f[0]) s1 f[1]) s2 f[2]) s3 f[3]) s4 f[4]) s5 f[5]) s6 f[6]) s7 f[7])
+            float hx[4], hy[4], hz[4];
+            hx[0] = HMOD(x, +, +, -, -, -, -, +, +);
+            hy[0] = HMOD(y, +, +, -, -, -, -, +, +);
+            hz[0] = HMOD(z, +, +, -, -, -, -, +, +);
+            hx[1] = HMOD(x, +, -, -, +, -, +, +, -);
+            hy[1] = HMOD(y, +, -, -, +, -, +, +, -);
+            hz[1] = HMOD(z, +, -, -, +, -, +, +, -);
+            hx[2] = HMOD(x, +, -, +, -, +, -, +, -);
+            hy[2] = HMOD(y, +, -, +, -, +, -, +, -);
+            hz[2] = HMOD(z, +, -, +, -, +, -, +, -);
+            hx[3] = HMOD(x, -, +, -, +, +, -, +, -);
+            hy[3] = HMOD(y, -, +, -, +, +, -, +, -);
+            hz[3] = HMOD(z, -, +, -, +, +, -, +, -);
+#undef HMOD
+            const float gam[4][8] = {
+                { 1.f,  1.f, -1.f, -1.f, -1.f, -1.f,  1.f,  1.f},
+                { 1.f, -1.f, -1.f,  1.f, -1.f,  1.f,  1.f, -1.f},
+                { 1.f, -1.f,  1.f, -1.f,  1.f, -1.f,  1.f, -1.f},
+                {-1.f,  1.f, -1.f,  1.f,  1.f, -1.f,  1.f, -1.f}};
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    hg[c][m] = gam[m][c] - volinv * (dvdx[c] * hx[m] + dvdy[c] * hy[m] + dvdz[c] * hz[m]);
+        }
+        const float coefficient =
+            (((-hourg) * 0.01f) * d2f(d.ss[k])) * d2f(d.elem_mass[k]) / cbrtf(determ);
+        // velocities relative to corner 0: the hourglass modes are blind to
+        // a uniform velocity (sum over corners of each hourgam column is 0)
+        const float2 *vel[3] = {d.xds, d.yds, d.zds};
+#pragma unroll
+        for (int dim = 0; dim < 3; ++dim) {
+            float u[8];
+            rel8(vel[dim], nl, u);
+            float h[4];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                float acc = hg[1][m] * u[1];
+#pragma unroll
+                for (int c = 2; c < 8; ++c) acc = acc + hg[c][m] * u[c];
+                h[m] = acc;
+            }
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                f[dim][c] += coefficient * (((hg[c][0] * h[0] + hg[c][1] * h[1]) + hg[c][2] * h[2]) + hg[c][3] * h[3]);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        d.f32x[c * ne + k] = f[0][c];
+        d.f32y[c * ne + k] = f[1][c];
+        d.f32z[c * ne + k] = f[2][c];
+    }
+}
+
+__global__ void __launch_bounds__(kBlockElem) k_elem_force_split(const __grid_constant__ Dom d)
+{
+    if (skip_step(d)) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.ne) return;
+    elem_force_split(d, k, d.sc);
+}
+
+// ---------------------------------------------------------------------
+// Node update: compensated gather, FP64 integration
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void kahan_add(float &s, float &c, float v)
+{
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+__device__ __forceinline__ void node_update_split(const Dom &d, int n, const DevScalars *sc)
+{
+
+    const int st = __ldg(d.corner_start + n), en = __ldg(d.corner_start + n + 1);
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    for (int i = st; i < en; ++i) {
+        const int c = __ldg(d.corner_list + i);
+        kahan_add(sx, cx, d.f32x[c]);
+        kahan_add(sy, cy, d.f32y[c]);
+        kahan_add(sz, cz, d.f32z[c]);
+    }
+    const double fx = f2d(sx) - f2d(cx);
+    const double fy = f2d(sy) - f2d(cy);
+    const double fz = f2d(sz) - f2d(cz);
+    if (d.keep & 1) {
+        d.fx[n] = fx;
+        d.fy[n] = fy;
+        d.fz[n] = fz;
+    }
+    const double dt = sc->deltatime, u_cut = d.prm.u_cut;
+    const double im = d.inv_mass[n];
+    const unsigned bc = __ldg(d.node_bc + n);
+    const double ax = (bc & 1) ? 0.0 : fx * im;
+    const double ay = (bc & 2) ? 0.0 : fy * im;
+    const double az = (bc & 4) ? 0.0 : fz * im;
+    double t, p;
+    t = d.xd[n] + ax * dt; if (fabs(t) < u_cut) t = 0.0; p = d.x[n] + t * dt;
+    d.xd[n] = t; d.x[n] = p; d.xds[n] = split_hi_lo(t); d.xs[n] = split_hi_lo(p);
+    t = d.yd[n] + ay * dt; if (fabs(t) < u_cut) t = 0.0; p = d.y[n] + t * dt;
+    d.yd[n] = t; d.y[n] = p; d.yds[n] = split_hi_lo(t); d.ys[n] = split_hi_lo(p);
+    t = d.zd[n] + az * dt; if (fabs(t) < u_cut) t = 0.0; p = d.z[n] + t * dt;
+    d.zd[n] = t; d.z[n] = p; d.zds[n] = split_hi_lo(t); d.zs[n] = split_hi_lo(p);
+}
+
+__global__ void __launch_bounds__(kBlockNode) k_node_update_split(const __grid_constant__ Dom d)
+{
+    if (skip_step(d)) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nn) return;
+    node_update_split(d, n, d.sc);
+}
+
+// ---------------------------------------------------------------------
+// Element kinematics: FP64 volume and strain rate, FP32 length and Q
+// gradients
+// ---------------------------------------------------------------------
+__device__ __forceinline__ float sum4f(float a, float b, float c, float e) { return ((a + b) + c) + e; }
+
+__device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevScalars *sc)
+{
+    const size_t ne = (size_t)d.ne;
+
+    int nl[8];
+    load_nodelist(d.nodelist, k, nl);
+
+    // FP64: relative volume and its change (CalcKinematicsForElems :1950-1958)
+    const double volo = d.volo[k];
+    double volume, vdov;
+    {
+        double X[8], Y[8], Z[8], U[8], V[8], W[8];
+        gather8(d.x, nl, X);
+        gather8(d.y, nl, Y);
+        gather8(d.z, nl, Z);
+        volume = elem_volume(X, Y, Z);
+        // FP64: the strain rate at the half step (:1975-2020)
+        gather8(d.xd, nl, U);
+        gather8(d.yd, nl, V);
+        gather8(d.zd, nl, W);
+        const double dt2 = 0.5 * sc->deltatime;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            X[j] -= dt2 * U[j];
+            Y[j] -= dt2 * V[j];
+            Z[j] -= dt2 * W[j];
+        }
+        double b[3][4], detJ;
+        shape_derivs4(X, Y, Z, b, detJ);
+        const double inv = 1.0 / detJ;
+        const double *vel[3] = {U, V, W};
+        double dd[3];
+#pragma unroll
+        for (int dim = 0; dim < 3; ++dim) {
+            const double *u = vel[dim];
+            dd[dim] = inv * (((b[dim][0] * (u[0] - u[6]) + b[dim][1] * (u[1] - u[7])) +
+                              b[dim][2] * (u[2] - u[4])) + b[dim][3] * (u[3] - u[5]));
+        }
+        vdov = (dd[0] + dd[1]) + dd[2];
+    }
+    const double rel = volume / volo;
+    d.vnew[k] = rel;
+    d.delv[k] = rel - d.v[k];
+    d.vdov[k] = vdov;
+    if (rel <= 0.0) flag_error(sc, ERR_K3_VNEW, k);
+
+    // FP32: characteristic length and monotonic-Q gradients (:1821-1862,
+    // :2034-2180) on corner-0-relative coordinates
+    float x[8], y[8], z[8], xv[8], yv[8], zv[8];
+    rel8(d.xs, nl, x);
+    rel8(d.ys, nl, y);
+    rel8(d.zs, nl, z);
+    rel8(d.xds, nl, xv);
+    rel8(d.yds, nl, yv);
+    rel8(d.zds, nl, zv);
+    const float volf = d2f(volume);
+    d.arealg[k] = f2d(char_length<float>(x, y, z, volf));
+
+    const float ptiny = 1.e-36f;
+    const float vol = d2f(volume);
+    const float norm = 1.f / (vol + ptiny);
+#define DJ(f) (-0.25f * (sum4f(f[0], f[1], f[5], f[4]) - sum4f(f[3], f[2], f[6], f[7])))
+#define DI(f) ( 0.25f * (sum4f(f[1], f[2], f[6], f[5]) - sum4f(f[0], f[3], f[7], f[4])))
+#define DK(f) ( 0.25f * (sum4f(f[4], f[5], f[6], f[7]) - sum4f(f[0], f[1], f[2], f[3])))
+    const float dxj = DJ(x), dyj = DJ(y), dzj = DJ(z);
+    const float dxi = DI(x), dyi = DI(y), dzi = DI(z);
+    const float dxk = DK(x), dyk = DK(y), dzk = DK(z);
+    float ax, ay, az;
+    float *gq = d.gq;
+
+    ax = dyi * dzj - dzi * dyj;
+    ay = dzi * dxj - dxi * dzj;
+    az = dxi * dyj - dyi * dxj;
+    gq[5 * ne + k] = vol / sqrtf(ax * ax + ay * ay + az * az + ptiny);           // delx_zeta
+    ax *= norm; ay *= norm; az *= norm;
+    gq[2 * ne + k] = ax * DK(xv) + ay * DK(yv) + az * DK(zv);                   // delv_zeta
+
+    ax = dyj * dzk - dzj * dyk;
+    ay = dzj * dxk - dxj * dzk;
+    az = dxj * dyk - dyj * dxk;
+    gq[3 * ne + k] = vol / sqrtf(ax * ax + ay * ay + az * az + ptiny);           // delx_xi
+    ax *= norm; ay *= norm; az *= norm;
+    gq[0 * ne + k] = ax * DI(xv) + ay * DI(yv) + az * DI(zv);                   // delv_xi
+
+    ax = dyk * dzi - dzk * dyi;
+    ay = dzk * dxi - dxk * dzi;
+    az = dxk * dyi - dyk * dxi;
+    gq[4 * ne + k] = vol / sqrtf(ax * ax + ay * ay + az * az + ptiny);           // delx_eta
+    ax *= norm; ay *= norm; az *= norm;
+    gq[1 * ne + k] = ax * DJ(xv) + ay * DJ(yv) + az * DJ(zv);                   // delv_eta
+#undef DJ
+#undef DI
+#undef DK
+}
+
+__global__ void __launch_bounds__(kBlockElem) k_elem_kinematics_split(const __grid_constant__ Dom d)
+{
+    if (skip_step(d)) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.ne) return;
+    elem_kinematics_split(d, k, d.sc);
+}
+
+// ---------------------------------------------------------------------
+// Q limiter in FP32, EOS and constraints in FP64
+// ---------------------------------------------------------------------
+template <bool kConstraints>
+__device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScalars *sc,
+                                                    unsigned long long &kc, unsigned long long &kh)
+{
+    const lulesh_params &P = d.prm;
+    {
+        const size_t ne = (size_t)d.ne;
+        const float *dv_xi = d.gq, *dv_eta = d.gq + ne, *dv_zeta = d.gq + 2 * ne;
+        const int bc = __ldg(d.elem_bc + k);
+        const float lim = d2f(P.monoq_limiter_mult), maxs = d2f(P.monoq_max_slope);
+        const float phixi = limiter_phi<float>(dv_xi, k, bc & BC_XI_M, bc & BC_XI_P, BC_XI_M_SYMM,
+                                               BC_XI_M_FREE, BC_XI_P_SYMM, BC_XI_P_FREE,
+                                               __ldg(d.lxim + k), __ldg(d.lxip + k), lim, maxs);
+        const float phieta = limiter_phi<float>(dv_eta, k, bc & BC_ETA_M, bc & BC_ETA_P, BC_ETA_M_SYMM,
+                                                BC_ETA_M_FREE, BC_ETA_P_SYMM, BC_ETA_P_FREE,
+                                                __ldg(d.letam + k), __ldg(d.letap + k), lim, maxs);
+        const float phizeta = limiter_phi<float>(dv_zeta, k, bc & BC_ZETA_M, bc & BC_ZETA_P,
+                                                 BC_ZETA_M_SYMM, BC_ZETA_M_FREE, BC_ZETA_P_SYMM,
+                                                 BC_ZETA_P_FREE, __ldg(d.lzetam + k), __ldg(d.lzetap + k),
+                                                 lim, maxs);
+        const double vnew = d.vnew[k], vdov = d.vdov[k];
+        double qlin = 0., qquad = 0.;
+        if (!(vdov > 0.)) {
+            float dxi = dv_xi[k] * d.gq[3 * ne + k];
+            float deta = dv_eta[k] * d.gq[4 * ne + k];
+            float dzeta = dv_zeta[k] * d.gq[5 * ne + k];
+            if (dxi > 0.f) dxi = 0.f;
+            if (deta > 0.f) deta = 0.f;
+            if (dzeta > 0.f) dzeta = 0.f;
+            const float rho = d2f(d.elem_mass[k]) / (d2f(d.volo[k]) * d2f(vnew));
+            const float sl = (dxi * (1.f - phixi) + deta * (1.f - phieta)) + dzeta * (1.f - phizeta);
+            const float sq = (dxi * dxi * (1.f - phixi * phixi) + deta * deta * (1.f - phieta * phieta)) +
+                             dzeta * dzeta * (1.f - phizeta * phizeta);
+            qlin = f2d(-d2f(P.qlc_monoq) * rho * sl);
+            qquad = f2d(d2f(P.qqc_monoq) * rho * sq);
+        }
+        if (d.keep & 2) {
+            d.ql[k] = qlin;
+            d.qq[k] = qquad;
+        }
+        const double ssn = material_update(d, k, sc, vnew, qlin, qquad);
+        if (kConstraints) constraint_keys(ssn, vdov, d.arealg[k], P, kc, kh);
+    }
+}
+
+template <bool kConstraints>
+__global__ void __launch_bounds__(kBlockElem) k_elem_material_split(const __grid_constant__ Dom d)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long kc = ~0ULL, kh = ~0ULL;
+    if (k < d.ne && !skip_step(d)) elem_material_split<kConstraints>(d, k, d.sc, kc, kh);
+    if (kConstraints) block_min_publish(kc, kh, d.sc);
+}
+
+// ---------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------
+static inline unsigned blocks_for(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+void launch_split_sync(const Dom &d, cudaStream_t st)
+{
+    k_split_sync<<<blocks_for(d.nn, kBlockNode), kBlockNode, 0, st>>>(d);
+}
+
+void launch_lagrange_nodal_split(const Dom &d, cudaStream_t st)
+{
+    k_elem_force_split<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    k_node_update_split<<<blocks_for(d.nn, kBlockNode), kBlockNode, 0, st>>>(d);
+}
+
+void launch_lagrange_elements_split(const Dom &d, cudaStream_t st, bool with_constraints)
+{
+    k_elem_kinematics_split<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    if (with_constraints)
+        k_elem_material_split<true><<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    else
+        k_elem_material_split<false><<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+}
+
+void launch_run_body_split(const Dom &d, cudaStream_t st, cudaGraphConditionalHandle h, int *active)
+{
+    launch_time_increment(d, st);
+    launch_lagrange_nodal_split(d, st);
+    launch_lagrange_elements_split(d, st, true);
+    launch_run_epilogue(d, st, h, active);
+}
+
+void launch_cycle_timed_split(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTimedKernels + 1])
+{
+    cudaEventRecord(ev[0], st);
+    launch_time_increment(d, st);
+    cudaEventRecord(ev[1], st);
+    k_elem_force_split<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    cudaEventRecord(ev[2], st);
+    k_node_update_split<<<blocks_for(d.nn, kBlockNode), kBlockNode, 0, st>>>(d);
+    cudaEventRecord(ev[3], st);
+    k_elem_kinematics_split<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    cudaEventRecord(ev[4], st);
+    k_elem_material_split<true><<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    cudaEventRecord(ev[5], st);
+    launch_finalize(d, st);
+    cudaEventRecord(ev[6], st);
+}
+
+}  // namespace lulesh

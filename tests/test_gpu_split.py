@@ -1,0 +1,85 @@
+"""The split-precision step (FP32 geometry and forces, FP64 state) against
+the FP64 reference results.
+
+Bar: <= 1e-6 relative error in the final origin energy against the FP64
+oracle's answer, the same cycle count on the s=30 run to t = 1e-2, and
+FP32-level agreement of every phase.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import find_run, load_phases, rel_err
+
+pytestmark = pytest.mark.gpu
+
+E0_TOL = 1e-6          # final origin energy, relative (the split path's bar)
+PHASE_TOL = 2e-5       # per-phase fields, relative to the field's max |value| (FP32 geometry)
+
+
+def test_split_phases_close_to_reference(pkg):
+    s, cyc = 10, 150
+    st = load_phases(s, cyc)
+    with pkg.Lulesh(s, pkg.INIT_V2, pkg.SPLIT) as g:
+        g.keep_forces(True)
+        for k in ("x", "y", "z", "xd", "yd", "zd", "e", "p", "q", "v", "ss"):
+            g.set_field(k, st["start"][k])
+        sc = g.scalars
+        sc.time, sc.deltatime = st["start"]["time"], st["start"]["deltatime"]
+        sc.dtcourant, sc.dthydro, sc.cycle = st["start"]["dtcourant"], st["start"]["dthydro"], cyc
+        g.scalars = sc
+        g.time_increment()
+        g.lagrange_nodal()
+        for k in ("fx", "fy", "fz", "xd", "yd", "zd"):
+            err = rel_err(g.get_field(k), st["lagrange_nodal"][k])
+            assert err <= PHASE_TOL, (k, err)
+        for k in ("x", "y", "z"):   # FP64 positions moved by FP32-accurate velocities
+            assert rel_err(g.get_field(k), st["lagrange_nodal"][k]) <= 1e-7, k
+        g.lagrange_elements()
+        vscale = np.max(np.abs(st["lagrange_elements"]["vnew"]))
+        for k in ("vnew", "delv", "vdov", "e", "p", "q", "v", "ss", "arealg",
+                  "delv_xi", "delv_eta", "delv_zeta", "delx_xi", "delx_eta", "delx_zeta"):
+            err = rel_err(g.get_field(k), st["lagrange_elements"][k], vscale if k == "delv" else 0.0)
+            assert err <= PHASE_TOL, (k, err)
+
+
+def test_split_full_run_s30(pkg, answers):
+    ref = find_run(answers, 30, "v2", 0)
+    with pkg.Lulesh(30, pkg.INIT_V2, pkg.SPLIT) as g:
+        n = g.run()
+        e0 = g.origin_energy()
+        ma, ta, mr = g.symmetry()
+    err = abs(e0 - ref["origin_energy"]) / ref["origin_energy"]
+    assert n == ref["cycles"], (n, ref["cycles"])
+    assert err <= E0_TOL, err
+    assert mr <= 1e-5, mr
+
+
+def test_split_tracks_fp64_at_s192(pkg):
+    """s=192, 100 cycles: the four reported results of the split path against
+    the plain FP64 path on the same GPU."""
+    s, n = 192, 100
+    mesh = pkg.mesh_build(s, pkg.INIT_V2)
+    with pkg.Lulesh(s, pkg.INIT_V2, pkg.FP64) as a:
+        assert a.run(n) == n
+        ref = pkg.sedov_metrics(a, mesh)
+    with pkg.Lulesh(s, pkg.INIT_V2, pkg.SPLIT) as b:
+        assert b.run(n) == n
+        got = pkg.sedov_metrics(b, mesh)
+    errs = pkg.relative_errors(got, ref)
+    assert errs["origin_energy"] <= E0_TOL, errs
+    assert errs["total_energy"] <= 1e-6, errs
+    assert errs["max_velocity"] <= 1e-5, errs
+    assert errs["shock_radius"] <= 1e-5, errs
+
+
+def test_split_deterministic_and_step_calls_equal_run(pkg):
+    n = 40
+    with pkg.Lulesh(12, pkg.INIT_V2, pkg.SPLIT) as a, pkg.Lulesh(12, pkg.INIT_V2, pkg.SPLIT) as b:
+        assert a.run(n) == n
+        for _ in range(n):
+            b.time_increment()
+            b.lagrange_leapfrog()
+        for k in ("x", "xd", "e", "p", "q", "v", "ss"):
+            assert np.array_equal(a.get_field(k), b.get_field(k)), k
