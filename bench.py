@@ -156,6 +156,92 @@ def cpu_run(s: int, warmup: int, cycles: int, threads: int) -> dict:
                       f"{warmup} warm-up cycles, {r['threads']} OpenMP threads"}
 
 
+def batch_legs(pkg, torch, args, barrier, max_over_ranks) -> dict:
+    """Configs 3 and 4: seeded ensembles run to t = 1e-2 in one captured graph
+    (c3: 64 instances, plain FP64; c4: 528 instances, split precision),
+    against the same instances run one at a time on the plain FP64 path
+    (a time-bounded sample of them, since the rate is what is compared)."""
+    import numpy as np
+
+    fx = json.loads((ROOT / "tests" / "golden" / "ensembles.json").read_text())
+    cache = ROOT / "lulesh-accelerate_gb300" / "_build" / "batch_tuning.json"
+    cache.parent.mkdir(exist_ok=True)
+    out = {}
+    for name, prec_name in (("c3", "fp64"), ("c4", "split")):
+        prec = pkg.FP64 if prec_name == "fp64" else pkg.SPLIT
+        sizes, scale = fx[name]["sizes"], fx[name]["e0_scale"]
+        with pkg.Batch(sizes, scale, pkg.INIT_V2, prec) as w:        # warm-up + tuning
+            w.autotune(str(cache))
+            w.run(args.warmup)
+        b = pkg.Batch(sizes, scale, pkg.INIT_V2, prec)
+        b.autotune(str(cache))
+        init = [b.instance(i) for i in range(b.n)]
+        st = torch.cuda.ExternalStream(b.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = b.kernel_launches
+        barrier()
+        e0.record(st)
+        most = b.run()
+        e1.record(st)
+        barrier()
+        ms = max_over_ranks(e0.elapsed_time(e1))
+        zc = b.zone_cycles()
+        final = [b.instance(i) for i in range(b.n)]
+        launches = b.kernel_launches - l0
+        tuning = b.tuning()
+        b.close()
+
+        # one at a time on the plain FP64 path: instances in order until the
+        # sample has run for --solo-seconds
+        solo_zc = solo_ms = 0.0
+        solo_n = 0
+        for i in range(len(sizes)):
+            g = pkg.Lulesh(int(sizes[i]), pkg.INIT_V2, pkg.FP64)
+            e = np.zeros(int(sizes[i]) ** 3)
+            e[0] = init[i][1]
+            g.set_field("e", e)
+            sc = g.scalars
+            sc.deltatime = init[i][0].deltatime
+            g.scalars = sc
+            gst = torch.cuda.ExternalStream(g.stream)
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record(gst)
+            n = g.run()
+            a1.record(gst)
+            torch.cuda.synchronize()
+            solo_ms += a0.elapsed_time(a1)
+            solo_zc += float(sizes[i]) ** 3 * n
+            solo_n += 1
+            g.close()
+            if solo_ms > 1e3 * args.solo_seconds:
+                break
+        solo_rate = solo_zc / (solo_ms * 1e-3) * 1e-6
+        value = zc / (ms * 1e-3) * 1e-6
+        leg = {"instances": len(sizes), "precision": prec_name, "elements": int(sum(int(x) ** 3 for x in sizes)),
+               "seed": fx[name]["seed"], "cycles_max": most, "zone_cycles": zc, "ms": ms,
+               "value": value, "unit": UNIT, "instances_per_s": len(sizes) / (ms * 1e-3),
+               "one_at_a_time_fp64": {"value": solo_rate, "unit": UNIT, "instances_sampled": solo_n,
+                                      "ms": solo_ms},
+               "speedup_vs_one_at_a_time_fp64": value / solo_rate, "gpu_launches": launches,
+               "autotuned": tuning}
+
+        if prec_name == "split":
+            # per-instance origin-energy error against FP64: one s=96
+            # instance and the first 32 smaller ones, run as an FP64 batch
+            idx = [i for i, x in enumerate(sizes) if x <= 48][:32] + [i for i, x in enumerate(sizes) if x > 48][:1]
+            with pkg.Batch([sizes[i] for i in idx], [scale[i] for i in idx], pkg.INIT_V2, pkg.FP64) as r:
+                r.autotune(str(cache))
+                r.run()
+                errs = []
+                for j, i in enumerate(idx):
+                    rsc, re0, _ = r.instance(j)
+                    errs.append(abs(final[i][1] - re0) / abs(re0))
+            leg["origin_energy_error_vs_fp64"] = {"max": max(errs), "median": float(np.median(errs)),
+                                                   "instances_compared": len(idx)}
+        out[name] = leg
+    return out
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -201,6 +287,9 @@ def main():
     ap.add_argument("--cpu-cycles", type=int, default=8, help="cycles of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-split", action="store_true", help="skip the split-precision leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble legs")
+    ap.add_argument("--solo-seconds", type=float, default=8.0,
+                    help="budget of the one-at-a-time sample of each batched leg")
     ap.add_argument("--launch", default="graph", choices=["graph", "direct"],
                     help="graph: the captured run loop (product path); direct: the same kernels "
                          "launched one by one (used for ncu captures)")
@@ -334,6 +423,10 @@ def main():
                  "roofline": sroof, "kernels": skernels, "bytes_per_zone_cycle": sbytes,
                  "dtype": "f32 geometry/forces/Q, f64 state/EOS/volume/vdov/dt"}
 
+    batched = None
+    if args.precision == "fp64" and not args.no_batch:
+        batched = batch_legs(pkg, torch, args, barrier, max_over_ranks)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_run(args.size, 2, args.cpu_cycles, os.cpu_count() or 1)
@@ -348,7 +441,8 @@ def main():
                          "note": "the FP64 pipe, not HBM, bounds this path: see kernels[*].gbs"},
                 "bytes_per_zone_cycle": cycle_bytes,
                 "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clocks.summary(), "results": ref_metrics, "split": split}
+                "clocks": clocks.summary(), "results": ref_metrics, "split": split,
+                "batched": batched}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

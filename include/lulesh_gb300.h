@@ -224,6 +224,51 @@ int lulesh_lagrange_nodal_noalloc(
     double *x, double *y, double *z, double *xd, double *yd, double *zd,
     double *fx, double *fy, double *fz, void *stream);
 
+/* ---- batched ensembles -------------------------------------------------
+ * Many independent Sedov problems of uneven size advanced together on one
+ * GPU, each with its own time, time step and stop time (the reference runs
+ * one problem per process; its MPI variants decompose one problem, they do
+ * not batch several).  Instance i has edge length sizes[i] and initial
+ * energy e0(s_i) * e0_scale[i] (e0_scale may be NULL for 1.0); with
+ * LULESH_INIT_V2 its initial time step is 0.5*cbrt(volo0)/sqrt(2*e0) of the
+ * scaled energy.  Every instance's arithmetic is exactly that of a
+ * single-instance context with the same initial state.  The batch runs as
+ * one CUDA graph; per size class of instance (s <= 24, s <= 48, larger) each
+ * step kernel has its own launch shape. */
+typedef struct lulesh_batch lulesh_batch;
+
+int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int init_mode, int precision,
+                        const lulesh_params *params, lulesh_batch **out);
+void lulesh_batch_destroy(lulesh_batch *b);
+const char *lulesh_batch_last_error(const lulesh_batch *b);
+
+/* Run every instance until its time reaches stoptime (the main loop of
+ * LULESH-OMP.cc:3179-3188 per instance), at most max_cycles cycles each
+ * (<= 0: no cap).  *cycles_done receives the largest per-instance count. */
+int lulesh_batch_run(lulesh_batch *b, int max_cycles, int *cycles_done);
+
+/* Counts; the per-instance state and status (LULESH_OK, LULESH_VOLUME_ERROR
+ * or LULESH_QSTOP_ERROR) and fields (the names of lulesh_get_field: "x" "y"
+ * "z" "xd" "yd" "zd" "e" "p" "q" "v" "ss" "vdov" "arealg" "volo" "elemMass"
+ * "nodalMass"). */
+int lulesh_batch_size(lulesh_batch *b, int *n, long *total_elements, long *total_nodes);
+int lulesh_batch_instance(lulesh_batch *b, int i, lulesh_scalars *out, double *origin_energy, int *status);
+int lulesh_batch_get_field(lulesh_batch *b, int i, const char *name, double *host, long n);
+/* Sum over instances of elements x cycles done. */
+int lulesh_batch_zone_cycles(lulesh_batch *b, double *zone_cycles);
+
+/* Choose threads per block (64/128/256, i.e. 4/2/1 elements per thread of a
+ * 256-element tile) and resident blocks per SM (1/2/4/8) of each step kernel
+ * per size class by timing the candidates on this batch, whose state is
+ * restored afterwards.  Choices are cached in the JSON file cache_path
+ * (keyed by GPU model, SM count, precision, class, kernel; NULL: no cache);
+ * retune != 0 ignores cached entries. */
+int lulesh_batch_autotune(lulesh_batch *b, const char *cache_path, int retune);
+int lulesh_batch_tuning(lulesh_batch *b, int size_class, int kernel, int *block, int *grid);
+
+void *lulesh_batch_stream(lulesh_batch *b);
+long long lulesh_batch_kernel_launches(lulesh_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

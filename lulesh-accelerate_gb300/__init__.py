@@ -32,6 +32,7 @@ __all__ = [
     "Parameters", "Domain", "Scalars", "Lulesh", "lulesh", "library_path", "load_library",
     "LuleshError", "VolumeError", "QStopError", "mesh_build", "mesh_sizes", "default_parameters",
     "INIT_V1", "INIT_V2", "FP64", "SPLIT", "sedov_metrics", "relative_errors", "probe_fp64_peak",
+    "Batch", "ensemble",
 ]
 
 _PKG = Path(__file__).resolve().parent
@@ -121,6 +122,19 @@ _SIGNATURES = {
     "lulesh_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "lulesh_run_profiled": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),
     "lulesh_probe_fp64_peak": (C.c_int, [_dp]),
+    "lulesh_batch_create": (C.c_int, [C.c_int, _ip, _dp, C.c_int, C.c_int, C.POINTER(Parameters),
+                                      C.POINTER(C.c_void_p)]),
+    "lulesh_batch_destroy": (None, [C.c_void_p]),
+    "lulesh_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "lulesh_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "lulesh_batch_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_long), C.POINTER(C.c_long)]),
+    "lulesh_batch_instance": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Scalars), _dp, C.POINTER(C.c_int)]),
+    "lulesh_batch_get_field": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, _dp, C.c_long]),
+    "lulesh_batch_zone_cycles": (C.c_int, [C.c_void_p, _dp]),
+    "lulesh_batch_autotune": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
+    "lulesh_batch_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "lulesh_batch_stream": (C.c_void_p, [C.c_void_p]),
+    "lulesh_batch_kernel_launches": (C.c_longlong, [C.c_void_p]),
 }
 
 TIMED_KERNELS = ("time_increment", "elem_force", "node_update", "elem_kinematics",
@@ -362,6 +376,110 @@ class Lulesh:
     @property
     def kernel_launches(self) -> int:
         return load_library().lulesh_kernel_launches(self._h)
+
+
+def _check_batch(rc: int, handle=None):
+    if rc == OK:
+        return
+    msg = load_library().lulesh_batch_last_error(handle).decode(errors="replace")
+    raise LuleshError(rc, msg)
+
+
+BATCH_KERNELS = ("elem_force", "node_update", "elem_kinematics", "elem_material")
+
+
+class Batch:
+    """An ensemble of independent Sedov problems advanced together on the GPU.
+
+    ``sizes[i]`` is instance i's edge length and ``e0_scale[i]`` multiplies
+    its initial energy.  Every instance runs to its own stop time with its
+    own time step; its arithmetic is that of a single :class:`Lulesh` started
+    from the same state.
+    """
+
+    def __init__(self, sizes, e0_scale=None, init: int = INIT_V2, precision: int = FP64,
+                 params: Parameters | None = None):
+        lib = load_library()
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+        scale = None if e0_scale is None else np.ascontiguousarray(e0_scale, dtype=np.float64)
+        h = C.c_void_p()
+        rc = lib.lulesh_batch_create(len(self.sizes), _ptr(self.sizes, C.c_int), _ptr(scale), init, precision,
+                                     C.byref(params) if params is not None else None, C.byref(h))
+        _check_batch(rc)
+        self._h = h
+        self.n = len(self.sizes)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().lulesh_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def run(self, max_cycles: int = 0) -> int:
+        n = C.c_int()
+        _check_batch(load_library().lulesh_batch_run(self._h, max_cycles, C.byref(n)), self._h)
+        return n.value
+
+    def instance(self, i: int) -> tuple[Scalars, float, int]:
+        sc, e0, st = Scalars(), C.c_double(), C.c_int()
+        _check_batch(load_library().lulesh_batch_instance(self._h, i, C.byref(sc), C.byref(e0), C.byref(st)),
+                     self._h)
+        return sc, e0.value, st.value
+
+    def get_field(self, i: int, name: str) -> np.ndarray:
+        s = int(self.sizes[i])
+        n = (s + 1) ** 3 if name in NODE_FIELDS else s ** 3
+        out = np.empty(n)
+        _check_batch(load_library().lulesh_batch_get_field(self._h, i, name.encode(), _ptr(out), n), self._h)
+        return out
+
+    def zone_cycles(self) -> float:
+        zc = C.c_double()
+        _check_batch(load_library().lulesh_batch_zone_cycles(self._h, C.byref(zc)), self._h)
+        return zc.value
+
+    def autotune(self, cache_path: str | None = None, retune: bool = False):
+        path = None if cache_path is None else str(cache_path).encode()
+        _check_batch(load_library().lulesh_batch_autotune(self._h, path, int(retune)), self._h)
+
+    def tuning(self) -> dict:
+        out = {}
+        for cls in range(3):
+            for k, name in enumerate(BATCH_KERNELS):
+                b, g = C.c_int(), C.c_int()
+                load_library().lulesh_batch_tuning(self._h, cls, k, C.byref(b), C.byref(g))
+                out[f"class{cls}/{name}"] = {"block": b.value, "grid": g.value}
+        return out
+
+    @property
+    def stream(self) -> int:
+        return load_library().lulesh_batch_stream(self._h) or 0
+
+    @property
+    def kernel_launches(self) -> int:
+        return load_library().lulesh_batch_kernel_launches(self._h)
+
+
+def ensemble(seed: int, n: int, lo: int, hi: int, extra_sizes=()) -> tuple[np.ndarray, np.ndarray]:
+    """Seeded ensemble of Sedov instances: n sizes uniform in lo..hi, then the
+    ``extra_sizes``, and one energy factor per instance, log-uniform in
+    [0.5, 2] (sizes drawn first, then factors, from
+    numpy.random.default_rng(seed))."""
+    rng = np.random.default_rng(seed)
+    sizes = np.concatenate([rng.integers(lo, hi + 1, n), np.asarray(extra_sizes, dtype=np.int64)])
+    factors = np.exp(rng.uniform(np.log(0.5), np.log(2.0), len(sizes)))
+    return sizes.astype(np.int32), factors
 
 
 def sedov_metrics(ctx: "Lulesh", mesh: dict | None = None) -> dict:

@@ -22,7 +22,7 @@ LIB = PKG / "liblulesh_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
            "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", str(PKG.parent / "include")]
-SOURCES = ["api.cu", "step_fp64.cu", "step_split.cu", "mesh.cpp", "noalloc.cu"]
+SOURCES = ["api.cu", "step_fp64.cu", "step_split.cu", "batch.cu", "mesh.cpp", "noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -36,4 +36,13 @@ void launch_lagrange_elements_split(const Dom &d, cudaStream_t st, bool with_con
 void launch_run_body_split(const Dom &d, cudaStream_t st, cudaGraphConditionalHandle h, int *active);
 void launch_cycle_timed_split(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTimedKernels + 1]);
 
+// Batched ensembles (batch.cu drives these; kernel ids 0..3 = force, node
+// update, kinematics, material).
+void launch_batch_kernel_fp64(const Dom &d, const BatchView &b, cudaStream_t st, int kernel, int cls,
+                              LaunchCfg cfg);
+void launch_batch_kernel_split(const Dom &d, const BatchView &b, cudaStream_t st, int kernel, int cls,
+                               LaunchCfg cfg);
+int batch_max_blocks_fp64(int kernel, int block);
+int batch_max_blocks_split(int kernel, int block);
+
 }  // namespace lulesh

@@ -96,4 +96,31 @@ struct Dom {
     lulesh_params prm;
 };
 
+// ---- batched ensembles -------------------------------------------------
+// Many independent Sedov instances share flat arrays: each instance's nodes
+// and elements occupy a range that starts on a multiple of kTile, so every
+// tile of kTile elements (or nodes) belongs to exactly one instance.  Tiles
+// are grouped into size classes, each with its own launch shape.
+constexpr int kTile = 256;
+constexpr int kMaxClasses = 3;
+constexpr int kBatchKernels = 4;   // force, node update, kinematics, material
+
+struct BatchView {
+    int n_inst, n_classes, n_etiles, n_ntiles;
+    const int *etile_inst, *ntile_inst;          // instance of each tile
+    const int *etile_class, *ntile_class;        // size class of each tile
+    const int *inst_elem_end, *inst_node_end;    // one past the instance's last element / node
+    const int *eclass_off, *nclass_off;          // start of each class's active list
+    int *active_etiles, *active_ntiles;          // active tiles, grouped by class
+    // counts[c] / counts[kMaxClasses + c]: active element / node tiles of
+    // class c; counts[2*kMaxClasses]: rebuild the lists; [2*kMaxClasses+1]:
+    // instances still running
+    int *counts;
+    unsigned char *inst_active;
+};
+
+struct LaunchCfg {
+    int block, grid;
+};
+
 }  // namespace lulesh

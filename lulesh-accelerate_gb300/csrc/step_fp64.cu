@@ -25,6 +25,7 @@
 #include "kernels.h"
 #include "geometry.cuh"
 #include "common.cuh"
+#include "batch_kernels.cuh"
 
 #include <cuda_runtime.h>
 
@@ -491,6 +492,34 @@ __global__ void k_fp64_probe(double *out, int iters, double a, double b)
 void launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t st)
 {
     k_fp64_probe<<<blocks, threads, 0, st>>>(out, iters, 0.999999, 1e-7);
+}
+
+// ---------------------------------------------------------------------
+// Batched ensembles: the same bodies over the active tiles of one class
+// ---------------------------------------------------------------------
+void launch_batch_kernel_fp64(const Dom &d, const BatchView &b, cudaStream_t st, int kernel, int cls,
+                              LaunchCfg cfg)
+{
+    switch (kernel) {
+    case 0: kb_elem<elem_force_fp64><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    case 1: kb_node<node_update_fp64><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    case 2: kb_elem<elem_kinematics_fp64><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    default: kb_material<elem_material_fp64<true>><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    }
+}
+
+// Resident blocks per SM of a batched kernel at a block size.
+int batch_max_blocks_fp64(int kernel, int block)
+{
+    int n = 0;
+    cudaError_t e;
+    switch (kernel) {
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_force_fp64>, block, 0); break;
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_node<node_update_fp64>, block, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_kinematics_fp64>, block, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material<elem_material_fp64<true>>, block, 0); break;
+    }
+    return e == cudaSuccess ? n : 0;
 }
 
 }  // namespace lulesh

@@ -25,6 +25,7 @@
 #include "kernels.h"
 #include "geometry.cuh"
 #include "common.cuh"
+#include "batch_kernels.cuh"
 
 #include <cuda_runtime.h>
 
@@ -470,6 +471,34 @@ void launch_cycle_timed_split(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTim
     cudaEventRecord(ev[5], st);
     launch_finalize(d, st);
     cudaEventRecord(ev[6], st);
+}
+
+// ---------------------------------------------------------------------
+// Batched ensembles: the same bodies over the active tiles of one class
+// ---------------------------------------------------------------------
+void launch_batch_kernel_split(const Dom &d, const BatchView &b, cudaStream_t st, int kernel, int cls,
+                              LaunchCfg cfg)
+{
+    switch (kernel) {
+    case 0: kb_elem<elem_force_split><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    case 1: kb_node<node_update_split><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    case 2: kb_elem<elem_kinematics_split><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    default: kb_material<elem_material_split<true>><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    }
+}
+
+// Resident blocks per SM of a batched kernel at a block size.
+int batch_max_blocks_split(int kernel, int block)
+{
+    int n = 0;
+    cudaError_t e;
+    switch (kernel) {
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_force_split>, block, 0); break;
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_node<node_update_split>, block, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_kinematics_split>, block, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material<elem_material_split<true>>, block, 0); break;
+    }
+    return e == cudaSuccess ? n : 0;
 }
 
 }  // namespace lulesh

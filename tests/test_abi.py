@@ -71,3 +71,18 @@ def test_create_fails_loudly_without_gpu(pkg):
     with pytest.raises(pkg.LuleshError) as ei:
         pkg.Lulesh(4)
     assert ei.value.code == pkg.ERR_CUDA
+
+
+def test_ensemble_fixture_is_the_seeded_draw(pkg):
+    """tests/golden/ensembles.json holds the seeded draws of the batched
+    configurations (c3: 64 instances s in 16..64, seed 0; c4: 512 in 8..48
+    plus 16 at s=96, seed 1; energy factors log-uniform in [0.5, 2])."""
+    import json
+
+    fx = json.loads((ROOT / "tests" / "golden" / "ensembles.json").read_text())
+    s3, f3 = pkg.ensemble(0, 64, 16, 64)
+    assert fx["c3"]["sizes"] == s3.tolist() and fx["c3"]["e0_scale"] == f3.tolist()
+    s4, f4 = pkg.ensemble(1, 512, 8, 48, (96,) * 16)
+    assert fx["c4"]["sizes"] == s4.tolist() and fx["c4"]["e0_scale"] == f4.tolist()
+    assert all(16 <= s <= 64 for s in s3) and all(0.5 <= f <= 2.0 for f in f3)
+    assert s4[-16:].tolist() == [96] * 16 and all(8 <= s <= 48 for s in s4[:512])

@@ -1,0 +1,89 @@
+"""Batched ensembles against single-instance runs and the oracle.
+
+Every instance of a batch must evolve exactly as a single-instance context
+started from the same state (bitwise: the same kernels and arithmetic, an
+order-free constraint minimum), reach its own stop time at its own cycle
+count, and match the oracle like any single run.
+"""
+from __future__ import annotations
+
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [4, 9, 6, 12, 5, 17]
+SCALE = [1.0, 0.7, 1.6, 1.0, 0.55, 1.9]
+
+
+def _solo_like(pkg, batch, i, precision):
+    """A single-instance context with batch instance i's initial state."""
+    s = int(batch.sizes[i])
+    sc, e0, _ = batch.instance(i)
+    g = pkg.Lulesh(s, pkg.INIT_V2, precision)
+    e = np.zeros(s ** 3)
+    e[0] = e0
+    g.set_field("e", e)
+    cur = g.scalars
+    cur.deltatime = sc.deltatime
+    g.scalars = cur
+    return g
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_batch_instances_equal_solo_runs(pkg, precision):
+    prec = pkg.FP64 if precision == "fp64" else pkg.SPLIT
+    with pkg.Batch(SIZES, SCALE, pkg.INIT_V2, prec) as b:
+        solos = [_solo_like(pkg, b, i, prec) for i in range(len(SIZES))]
+        most = b.run()
+        counts = []
+        for i, g in enumerate(solos):
+            n = g.run()
+            counts.append(n)
+            sc, e0, status = b.instance(i)
+            assert status == pkg.OK
+            assert sc.cycle == n, (i, sc.cycle, n)
+            assert sc.time == g.scalars.time
+            for k in ("x", "y", "z", "xd", "yd", "zd", "e", "p", "q", "v", "ss"):
+                assert np.array_equal(b.get_field(i, k), g.get_field(k)), (i, k)
+            g.close()
+        assert most == max(counts)
+        assert len(set(counts)) > 1          # instances really ran to different cycle counts
+        assert b.zone_cycles() == sum(s ** 3 * n for s, n in zip(SIZES, counts))
+
+
+def test_batch_instance_matches_oracle(pkg, orc):
+    """A scaled-energy instance against the oracle started from its state."""
+    with pkg.Batch([10, 7], [0.7, 1.3], pkg.INIT_V2, pkg.FP64) as b:
+        sc0, e00, _ = b.instance(0)
+        b.run()
+        sc, e0, _ = b.instance(0)
+    o = orc.Oracle(10, orc.INIT_V2)
+    o.field("e")[0] = e00
+    o.set_scalar("deltatime", sc0.deltatime)
+    rc, _ = o.run()
+    assert rc == 0
+    assert sc.cycle == o.cycle
+    assert abs(e0 - o.field("e")[0]) <= 1e-10 * abs(o.field("e")[0])
+
+
+def test_autotune_restores_state_and_caches(pkg, tmp_path):
+    cache = tmp_path / "tuning.json"
+    with pkg.Batch(SIZES, SCALE) as ref:
+        ref.run()
+        want = [ref.get_field(i, "e") for i in range(len(SIZES))]
+    with pkg.Batch(SIZES, SCALE) as b:
+        b.autotune(str(cache))
+        tuned = b.tuning()
+        b.run()
+        for i in range(len(SIZES)):
+            assert np.array_equal(b.get_field(i, "e"), want[i]), i
+    entries = json.loads(cache.read_text())
+    assert entries and all(v[0] in (64, 128, 256) for v in entries.values())
+    with pkg.Batch(SIZES, SCALE) as c:
+        c.autotune(str(cache))                 # served from the cache
+        assert c.tuning() == tuned
