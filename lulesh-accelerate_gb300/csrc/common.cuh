@@ -145,11 +145,18 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
     double compression = 1. / vnewc - 1.;
     const double vchalf = vnewc - delvc * .5;
     double comp_half = 1. / vchalf - 1.;
-    if (eosvmin != 0. && vnewc <= eosvmin) comp_half = compression;
+    // vhalf = 1 / (1 + comp_half) (:2460), which is vchalf, vnewc or 1 in the
+    // three cases below; taken directly instead of through two divisions
+    double vhalf = vchalf;
+    if (eosvmin != 0. && vnewc <= eosvmin) {
+        comp_half = compression;
+        vhalf = vnewc;
+    }
     if (eosvmax != 0. && vnewc >= eosvmax) {
         p_old = 0.;
         compression = 0.;
         comp_half = 0.;
+        vhalf = 1.;
     }
     const double rho0 = P.refdens;
     const bool unit_rho0 = (rho0 == 1.0);
@@ -160,7 +167,6 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
     double e_new = e_old - .5 * delvc * (p_old + q_old);
     if (e_new < emin) e_new = emin;
     const double p_half = eos_pressure(bvc, e_new, comp_half, vnewc, P);
-    const double vhalf = 1. / (1. + comp_half);
     double q_new = 0.;
     if (!(delvc > 0.)) q_new = sound_term(pbvc, e_new, vhalf, bvc, p_half, rho0, unit_rho0) * qlin + qquad;
     e_new = e_new + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (p_half + q_new));
@@ -251,8 +257,7 @@ __device__ __forceinline__ void constraint_keys(double ss, double vdov, double a
         const double qqc2 = 64.0 * P.qqc * P.qqc;
         double dtf = ss * ss;
         if (vdov < 0.) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
-        dtf = sqrt(dtf);
-        dtf = arealg / dtf;
+        dtf = arealg * rsqrt(dtf);      // arealg / sqrt(dtf)
         kc = order_key(dtf);
         kh = order_key(P.dvovmax / (fabs(vdov) + 1.e-20));
     }

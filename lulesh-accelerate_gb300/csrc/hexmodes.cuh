@@ -1,0 +1,192 @@
+// hexmodes.cuh -- hexahedron geometry through the Walsh modes of its corners.
+//
+// A trilinear hexahedron x(xi,eta,zeta), xi,eta,zeta in [-1,1], with the
+// reference's corner order (corner c at signs s(c) = (-,-,-) (+,-,-) (+,+,-)
+// (-,+,-) (-,-,+) (+,-,+) (+,+,+) (-,+,+)) is
+//     x = (M0 + M1 xi + M2 eta + M3 zeta + M4 xi eta + M5 xi zeta
+//          + M6 eta zeta + M7 xi eta zeta) / 8,
+// where the modes M_i = sum_c s_i(c) x_c are the Walsh transform of the
+// corner coordinates (three butterfly stages, 24 additions).  Everything the
+// step needs from the corner coordinates is a short expression in these
+// modes:
+//   - the Jacobian columns at the centre (CalcElemShapeFunctionDerivatives,
+//     LULESH-OMP.cc:650-660) are M1/8, M2/8, M3/8;
+//   - the monotonic-Q logical differences (:2066-2076) are M1/4, M2/4, M3/4;
+//   - the four hourglass base vectors gamma (:1252-1285) are the sign
+//     patterns eta zeta, xi zeta, xi eta, xi eta zeta, so the hourglass mode
+//     projections sum_c gamma_m(c) x_c are M6, M5, M4, M7;
+//   - the exact volume (CalcElemVolume, :1706-1790) integrates det J over the
+//     cube: V = [M1.(M2xM3) + (M4.(M2xM6) + M5.(M6xM3) + M1.(M4xM5))/3] / 64;
+//   - its derivative with respect to corner c (CalcElemVolumeDerivative,
+//     :1008-1048) is (1/64) sum_{i=1..6} s_i(c) W_i with the W_i below, an
+//     inverse Walsh transform of six vectors.
+// These are the reference's quantities, not approximations of them; only the
+// rounding differs (relative differences of a few 1e-16 on distorted
+// elements, checked against the reference formulas).
+#pragma once
+
+namespace lulesh {
+
+template <typename T>
+struct V3 {
+    T x, y, z;
+};
+
+template <typename T>
+__device__ __forceinline__ V3<T> cross3(const V3<T> &a, const V3<T> &b)
+{
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+template <typename T>
+__device__ __forceinline__ T dot3(const V3<T> &a, const V3<T> &b)
+{
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+
+// Modes m[0..6] = M1..M7 (xi, eta, zeta, xi eta, xi zeta, eta zeta,
+// xi eta zeta) of 8 corner values.
+template <typename T>
+__device__ __forceinline__ void walsh8(const T c[8], T m[7])
+{
+    const T s01 = c[0] + c[1], d01 = c[1] - c[0];
+    const T s32 = c[3] + c[2], d32 = c[2] - c[3];
+    const T s45 = c[4] + c[5], d45 = c[5] - c[4];
+    const T s76 = c[7] + c[6], d76 = c[6] - c[7];
+    const T ssm = s01 + s32, dsm = s32 - s01;    // zeta = -1 face
+    const T ssp = s45 + s76, dsp = s76 - s45;    // zeta = +1 face
+    const T sdm = d01 + d32, ddm = d32 - d01;
+    const T sdp = d45 + d76, ddp = d76 - d45;
+    m[0] = sdm + sdp;    // xi
+    m[1] = dsm + dsp;    // eta
+    m[2] = ssp - ssm;    // zeta
+    m[3] = ddm + ddp;    // xi eta
+    m[4] = sdp - sdm;    // xi zeta
+    m[5] = dsp - dsm;    // eta zeta
+    m[6] = ddp - ddm;    // xi eta zeta
+}
+
+// The three linear modes only (17 additions).
+template <typename T>
+__device__ __forceinline__ void walsh_linear(const T c[8], T m[3])
+{
+    const T s01 = c[0] + c[1], d01 = c[1] - c[0];
+    const T s32 = c[3] + c[2], d32 = c[2] - c[3];
+    const T s45 = c[4] + c[5], d45 = c[5] - c[4];
+    const T s76 = c[7] + c[6], d76 = c[6] - c[7];
+    m[0] = (d01 + d32) + (d45 + d76);
+    m[1] = (s32 - s01) + (s76 - s45);
+    m[2] = (s45 + s76) - (s01 + s32);
+}
+
+template <typename T>
+__device__ __forceinline__ V3<T> mode(const T mx[7], const T my[7], const T mz[7], int i)
+{
+    return {mx[i], my[i], mz[i]};
+}
+
+// 64 x volume of the trilinear hexahedron.
+template <typename T>
+__device__ __forceinline__ T volume64(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3, const V3<T> &M4,
+                                      const V3<T> &M5, const V3<T> &M6)
+{
+    const T third = T(1.0) / T(3.0);
+    const T bil = dot3(M4, cross3(M2, M6)) + dot3(M5, cross3(M6, M3)) + dot3(M1, cross3(M4, M5));
+    return dot3(M1, cross3(M2, M3)) + bil * third;
+}
+
+// Corner values of sum_{i=1..6} s_i(c) q_i (inverse Walsh transform with
+// the constant and xi eta zeta modes zero), 20 additions.
+template <typename T>
+__device__ __forceinline__ void inv_walsh6(T q1, T q2, T q3, T q4, T q5, T q6, T v[8])
+{
+    const T bp = q1 + q4, bm = q1 - q4;
+    const T cp = q3 + q6, cm = q3 - q6;
+    const T epp = q2 + bp, emp = q2 - bp;        // E(+,+), E(-,+)
+    const T epm = bm - q2, emm = -(q2 + bm);     // E(+,-), E(-,-)
+    const T fpp = cp + q5, fmp = cp - q5;        // F(+,+), F(-,+)
+    const T fpm = cm + q5, fmm = cm - q5;        // F(+,-), F(-,-)
+    v[0] = emm - fmm;
+    v[1] = epm - fpm;
+    v[2] = epp - fpp;
+    v[3] = emp - fmp;
+    v[4] = emm + fmm;
+    v[5] = epm + fpm;
+    v[6] = epp + fpp;
+    v[7] = emp + fmp;
+}
+
+// 64 x the volume derivative of each corner, D[c] = dV/dx_c * 64.
+template <typename T>
+__device__ __forceinline__ void volume_derivative64(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
+                                                    const V3<T> &M4, const V3<T> &M5, const V3<T> &M6,
+                                                    T dx[8], T dy[8], T dz[8])
+{
+    const T third = T(1.0) / T(3.0);
+    auto add3 = [](const V3<T> &a, const V3<T> &b, T s) {
+        return V3<T>{a.x + b.x * s, a.y + b.y * s, a.z + b.z * s};
+    };
+    auto sum3 = [](const V3<T> &a, const V3<T> &b, T s) {
+        return V3<T>{(a.x + b.x) * s, (a.y + b.y) * s, (a.z + b.z) * s};
+    };
+    const V3<T> W1 = add3(cross3(M2, M3), cross3(M4, M5), third);
+    const V3<T> W2 = add3(cross3(M3, M1), cross3(M6, M4), third);
+    const V3<T> W3 = add3(cross3(M1, M2), cross3(M5, M6), third);
+    const V3<T> W4 = sum3(cross3(M2, M6), cross3(M5, M1), third);
+    const V3<T> W5 = sum3(cross3(M6, M3), cross3(M1, M4), third);
+    const V3<T> W6 = sum3(cross3(M4, M2), cross3(M3, M5), third);
+    inv_walsh6(W1.x, W2.x, W3.x, W4.x, W5.x, W6.x, dx);
+    inv_walsh6(W1.y, W2.y, W3.y, W4.y, W5.y, W6.y, dy);
+    inv_walsh6(W1.z, W2.z, W3.z, W4.z, W5.z, W6.z, dz);
+}
+
+// Unscaled node normals: corner sums of v x u over the three faces of each
+// corner, u and v the face diagonals (8 x the reference's node normals,
+// :708-799).
+template <typename T>
+__device__ __forceinline__ void node_normals8(T pf[3][8], const T x[8], const T y[8], const T z[8])
+{
+    T a[6][3];
+    const int f[6][4] = {{0, 1, 2, 3}, {0, 4, 5, 1}, {1, 5, 6, 2}, {2, 6, 7, 3}, {3, 7, 4, 0}, {4, 7, 6, 5}};
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const int n0 = f[i][0], n1 = f[i][1], n2 = f[i][2], n3 = f[i][3];
+        const T ux = x[n2] - x[n0], uy = y[n2] - y[n0], uz = z[n2] - z[n0];
+        const T vx = x[n3] - x[n1], vy = y[n3] - y[n1], vz = z[n3] - z[n1];
+        a[i][0] = vy * uz - vz * uy;
+        a[i][1] = vz * ux - vx * uz;
+        a[i][2] = vx * uy - vy * ux;
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        pf[d][0] = (a[0][d] + a[1][d]) + a[4][d];
+        pf[d][1] = (a[0][d] + a[1][d]) + a[2][d];
+        pf[d][2] = (a[0][d] + a[2][d]) + a[3][d];
+        pf[d][3] = (a[0][d] + a[3][d]) + a[4][d];
+        pf[d][4] = (a[1][d] + a[4][d]) + a[5][d];
+        pf[d][5] = (a[1][d] + a[2][d]) + a[5][d];
+        pf[d][6] = (a[2][d] + a[3][d]) + a[5][d];
+        pf[d][7] = (a[3][d] + a[4][d]) + a[5][d];
+    }
+}
+
+// Largest |u x v|^2 over the six faces, u and v the face diagonals: the
+// reference's AreaFace (:1799-1819) is |f|^2|g|^2 - (f.g)^2 with f = u - v,
+// g = u + v, which equals 4|u x v|^2 (Lagrange's identity).
+template <typename T>
+__device__ __forceinline__ T max_face_cross2(const T x[8], const T y[8], const T z[8])
+{
+    const int f[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+    T m = T(0.0);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const int a = f[i][0], b = f[i][1], c = f[i][2], d = f[i][3];
+        const V3<T> u{x[c] - x[a], y[c] - y[a], z[c] - z[a]};
+        const V3<T> v{x[d] - x[b], y[d] - y[b], z[d] - z[b]};
+        const V3<T> w = cross3(u, v);
+        m = fmax(dot3(w, w), m);
+    }
+    return m;
+}
+
+}  // namespace lulesh

@@ -24,6 +24,7 @@
 #include "lulesh_internal.h"
 #include "kernels.h"
 #include "geometry.cuh"
+#include "hexmodes.cuh"
 #include "common.cuh"
 #include "batch_kernels.cuh"
 
@@ -46,28 +47,33 @@ __global__ void k_time_increment(const __grid_constant__ Dom d)
 __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars *sc)
 {
     const size_t ne = (size_t)d.ne;
-
     int nl[8];
     load_nodelist(d.nodelist, k, nl);
     double x[8], y[8], z[8];
     gather8(d.x, nl, x);
     gather8(d.y, nl, y);
     gather8(d.z, nl, z);
+    double mx[7], my[7], mz[7];
+    walsh8(x, mx);
+    walsh8(y, my);
+    walsh8(z, mz);
+    const V3<double> M1 = mode(mx, my, mz, 0), M2 = mode(mx, my, mz, 1), M3 = mode(mx, my, mz, 2);
 
     // IntegrateStressForElems (LULESH-OMP.cc:853-903): sig = -p - q and the
-    // corner force -sig * (area-weighted node normal).
+    // corner force -sig * (area-weighted node normal).  The Jacobian volume
+    // it checks is 8 t.(c x a) = M2.(M3 x M1) / 64; only its sign matters.
     {
-        const double determ = jacobian_volume(x, y, z);
+        const double determ64 = dot3(M2, cross3(M3, M1));
         double pf[3][8];
-        node_normals(pf, x, y, z);
-        const double sig = -d.p[k] - d.q[k];
+        node_normals8(pf, x, y, z);                      // 8 x the normals
+        const double sig8 = 0.125 * (-d.p[k] - d.q[k]);
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-            d.fsx[c * ne + k] = -(sig * pf[0][c]);
-            d.fsy[c * ne + k] = -(sig * pf[1][c]);
-            d.fsz[c * ne + k] = -(sig * pf[2][c]);
+            d.fsx[c * ne + k] = -(sig8 * pf[0][c]);
+            d.fsy[c * ne + k] = -(sig8 * pf[1][c]);
+            d.fsz[c * ne + k] = -(sig8 * pf[2][c]);
         }
-        if (determ <= 0.0) flag_error(sc, ERR_K1_DETERM, k);
+        if (determ64 <= 0.0) flag_error(sc, ERR_K1_DETERM, k);
     }
 
     // CalcHourglassControlForElems (:1503-1558)
@@ -86,43 +92,32 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
         return;
     }
 
-    // CalcFBHourglassForceForElems (:1291-1473)
+    // CalcFBHourglassForceForElems (:1291-1473): hourgam = gamma -
+    // volinv * (dV/dx . hourmod), with hourmod the gamma projections of the
+    // coordinates (modes M6, M5, M4, M7) and dV/dx from the modes.
+    const double r = rcbrt(determ);                       // determ^(-1/3)
+    const double volinv64 = (r * r * r) * (1.0 / 64.0);   // the 1/64 of volume_derivative64
     double hg[8][4];
     {
+        const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
+        const V3<double> M7 = mode(mx, my, mz, 6);
         double dvdx[8], dvdy[8], dvdz[8];
-        volume_derivative(dvdx, dvdy, dvdz, x, y, z);
-        const double volinv = 1.0 / determ;
-        // hourglass base vectors gamma (:1252-1285); products with +-1 are
-        // written as additions/subtractions, which is exact.
-#define HMOD(f, s0, s1, s2, s3, s4, s5, s6, s7) \
-        ((((((((s0 f[0]) s1 f[1]) s2 f[2]) s3 f[3]) s4 f[4]) s5 f[5]) s6 f[6]) s7 f[7])
-        double hx[4], hy[4], hz[4];
-        hx[0] = HMOD(x, +, +, -, -, -, -, +, +);
-        hy[0] = HMOD(y, +, +, -, -, -, -, +, +);
-        hz[0] = HMOD(z, +, +, -, -, -, -, +, +);
-        hx[1] = HMOD(x, +, -, -, +, -, +, +, -);
-        hy[1] = HMOD(y, +, -, -, +, -, +, +, -);
-        hz[1] = HMOD(z, +, -, -, +, -, +, +, -);
-        hx[2] = HMOD(x, +, -, +, -, +, -, +, -);
-        hy[2] = HMOD(y, +, -, +, -, +, -, +, -);
-        hz[2] = HMOD(z, +, -, +, -, +, -, +, -);
-        hx[3] = HMOD(x, -, +, -, +, +, -, +, -);
-        hy[3] = HMOD(y, -, +, -, +, +, -, +, -);
-        hz[3] = HMOD(z, -, +, -, +, +, -, +, -);
-#undef HMOD
+        volume_derivative64(M1, M2, M3, M4, M5, M6, dvdx, dvdy, dvdz);
+        const V3<double> H[4] = {M6, M5, M4, M7};
         const double gam[4][8] = {
             { 1.,  1., -1., -1., -1., -1.,  1.,  1.},
             { 1., -1., -1.,  1., -1.,  1.,  1., -1.},
             { 1., -1.,  1., -1.,  1., -1.,  1., -1.},
             {-1.,  1., -1.,  1.,  1., -1.,  1., -1.}};
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
+        for (int m = 0; m < 4; ++m) {
+            const double hx = volinv64 * H[m].x, hy = volinv64 * H[m].y, hz = volinv64 * H[m].z;
 #pragma unroll
             for (int c = 0; c < 8; ++c)
-                hg[c][m] = gam[m][c] - volinv * (dvdx[c] * hx[m] + dvdy[c] * hy[m] + dvdz[c] * hz[m]);
+                hg[c][m] = gam[m][c] - (dvdx[c] * hx + dvdy[c] * hy + dvdz[c] * hz);
+        }
     }
-    const double volume13 = cbrt(determ);
-    const double coefficient = -hourg * 0.01 * d.ss[k] * d.elem_mass[k] / volume13;
+    const double coefficient = -hourg * 0.01 * d.ss[k] * d.elem_mass[k] * r;
 
     // CalcElemFBHourglassForce (:1050-1231), one velocity component at a time
     const double *vel[3] = {d.xd, d.yd, d.zd};
@@ -137,12 +132,11 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
             double acc = hg[0][m] * u[0];
 #pragma unroll
             for (int c = 1; c < 8; ++c) acc = acc + hg[c][m] * u[c];
-            h[m] = acc;
+            h[m] = coefficient * acc;
         }
 #pragma unroll
         for (int c = 0; c < 8; ++c)
-            out[dim][c * ne + k] =
-                coefficient * (((hg[c][0] * h[0] + hg[c][1] * h[1]) + hg[c][2] * h[2]) + hg[c][3] * h[3]);
+            out[dim][c * ne + k] = ((hg[c][0] * h[0] + hg[c][1] * h[1]) + hg[c][2] * h[2]) + hg[c][3] * h[3];
     }
 }
 
@@ -201,89 +195,71 @@ __global__ void __launch_bounds__(kBlockNode) k_node_update(const __grid_constan
 // ---------------------------------------------------------------------
 // Element kinematics + monotonic-Q gradients
 // ---------------------------------------------------------------------
-__device__ __forceinline__ double sum4(double a, double b, double c, double e) { return ((a + b) + c) + e; }
-
 __device__ __forceinline__ void elem_kinematics_fp64(const Dom &d, int k, DevScalars *sc)
 {
-
     int nl[8];
     load_nodelist(d.nodelist, k, nl);
-    double x[8], y[8], z[8], xv[8], yv[8], zv[8];
+    double x[8], y[8], z[8];
     gather8(d.x, nl, x);
     gather8(d.y, nl, y);
     gather8(d.z, nl, z);
-    gather8(d.xd, nl, xv);
-    gather8(d.yd, nl, yv);
-    gather8(d.zd, nl, zv);
+    double mx[7], my[7], mz[7];
+    walsh8(x, mx);
+    walsh8(y, my);
+    walsh8(z, mz);
+    const V3<double> M1 = mode(mx, my, mz, 0), M2 = mode(mx, my, mz, 1), M3 = mode(mx, my, mz, 2);
+    double vx[3], vy[3], vz[3];
+    {
+        double u[8];
+        gather8(d.xd, nl, u);
+        walsh_linear(u, vx);
+        gather8(d.yd, nl, u);
+        walsh_linear(u, vy);
+        gather8(d.zd, nl, u);
+        walsh_linear(u, vz);
+    }
+    const V3<double> V1{vx[0], vy[0], vz[0]}, V2{vx[1], vy[1], vz[1]}, V3v{vx[2], vy[2], vz[2]};
 
     // CalcKinematicsForElems, volume part (:1950-1964)
     const double volo = d.volo[k];
-    const double volume = elem_volume(x, y, z);
+    const double volume =
+        volume64(M1, M2, M3, mode(mx, my, mz, 3), mode(mx, my, mz, 4), mode(mx, my, mz, 5)) * (1.0 / 64.0);
     const double rel = volume / volo;
     d.vnew[k] = rel;
     d.delv[k] = rel - d.v[k];
-    d.arealg[k] = char_length(x, y, z, volume);
+    // CalcElemCharacteristicLength (:1821-1862): 4V / sqrt(max 4|u x v|^2)
+    d.arealg[k] = (2.0 * volume) * rsqrt(max_face_cross2(x, y, z));
     if (rel <= 0.0) flag_error(sc, ERR_K3_VNEW, k);
 
-    // CalcMonotonicQGradientsForElems (:2034-2180) on the new positions
+    // CalcMonotonicQGradientsForElems (:2034-2180): the logical differences
+    // are M/4, so each cross product is (M x M')/16 and each velocity
+    // difference Mv/4.
     {
         const double ptiny = 1.e-36;
         const double vol = volo * rel;
         const double norm = 1.0 / (vol + ptiny);
-#define DJ(f) (-0.25 * (sum4(f[0], f[1], f[5], f[4]) - sum4(f[3], f[2], f[6], f[7])))
-#define DI(f) ( 0.25 * (sum4(f[1], f[2], f[6], f[5]) - sum4(f[0], f[3], f[7], f[4])))
-#define DK(f) ( 0.25 * (sum4(f[4], f[5], f[6], f[7]) - sum4(f[0], f[1], f[2], f[3])))
-        const double dxj = DJ(x), dyj = DJ(y), dzj = DJ(z);
-        const double dxi = DI(x), dyi = DI(y), dzi = DI(z);
-        const double dxk = DK(x), dyk = DK(y), dzk = DK(z);
-        double ax, ay, az;
-
-        ax = dyi * dzj - dzi * dyj;
-        ay = dzi * dxj - dxi * dzj;
-        az = dxi * dyj - dyi * dxj;
-        d.delx_zeta[k] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
-        ax *= norm; ay *= norm; az *= norm;
-        d.delv_zeta[k] = ax * DK(xv) + ay * DK(yv) + az * DK(zv);
-
-        ax = dyj * dzk - dzj * dyk;
-        ay = dzj * dxk - dxj * dzk;
-        az = dxj * dyk - dyj * dxk;
-        d.delx_xi[k] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
-        ax *= norm; ay *= norm; az *= norm;
-        d.delv_xi[k] = ax * DI(xv) + ay * DI(yv) + az * DI(zv);
-
-        ax = dyk * dzi - dzk * dyi;
-        ay = dzk * dxi - dxk * dzi;
-        az = dxk * dyi - dyk * dxi;
-        d.delx_eta[k] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
-        ax *= norm; ay *= norm; az *= norm;
-        d.delv_eta[k] = ax * DJ(xv) + ay * DJ(yv) + az * DJ(zv);
-#undef DJ
-#undef DI
-#undef DK
+        const double vscale = 0.015625 * norm;           // (1/16) (1/4) norm
+        const V3<double> Az = cross3(M1, M2), Ax = cross3(M2, M3), Ae = cross3(M3, M1);
+        d.delx_zeta[k] = vol * rsqrt(0.00390625 * dot3(Az, Az) + ptiny);
+        d.delv_zeta[k] = vscale * dot3(Az, V3v);
+        d.delx_xi[k] = vol * rsqrt(0.00390625 * dot3(Ax, Ax) + ptiny);
+        d.delv_xi[k] = vscale * dot3(Ax, V1);
+        d.delx_eta[k] = vol * rsqrt(0.00390625 * dot3(Ae, Ae) + ptiny);
+        d.delv_eta[k] = vscale * dot3(Ae, V2);
     }
 
-    // CalcKinematicsForElems, strain-rate part (:1975-2000) at the half step
+    // CalcKinematicsForElems, strain-rate part (:1975-2020): the Jacobian at
+    // the half step has columns (M - dt/2 Mv)/8; tr(grad v) = sum over
+    // cofactors x velocity modes / det.
     const double dt2 = 0.5 * sc->deltatime;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        x[j] -= dt2 * xv[j];
-        y[j] -= dt2 * yv[j];
-        z[j] -= dt2 * zv[j];
-    }
-    double b[3][4], detJ;
-    shape_derivs4(x, y, z, b, detJ);
-    const double inv = 1.0 / detJ;
-    const double *vel[3] = {xv, yv, zv};
-    double dd[3];
-#pragma unroll
-    for (int dim = 0; dim < 3; ++dim) {
-        const double *u = vel[dim];
-        dd[dim] = inv * (((b[dim][0] * (u[0] - u[6]) + b[dim][1] * (u[1] - u[7])) +
-                          b[dim][2] * (u[2] - u[4])) + b[dim][3] * (u[3] - u[5]));
-    }
-    // CalcLagrangeElements (:2013-2020): only the trace is read later
-    d.vdov[k] = (dd[0] + dd[1]) + dd[2];
+    const V3<double> A{M1.x - dt2 * V1.x, M1.y - dt2 * V1.y, M1.z - dt2 * V1.z};
+    const V3<double> T{M2.x - dt2 * V2.x, M2.y - dt2 * V2.y, M2.z - dt2 * V2.z};
+    const V3<double> C{M3.x - dt2 * V3v.x, M3.y - dt2 * V3v.y, M3.z - dt2 * V3v.z};
+    const V3<double> cxi = cross3(T, C), cet = cross3(C, A), cze = cross3(A, T);
+    const double num = (cxi.x * vx[0] + cet.x * vx[1] + cze.x * vx[2]) +
+                       (cxi.y * vy[0] + cet.y * vy[1] + cze.y * vy[2]) +
+                       (cxi.z * vz[0] + cet.z * vz[1] + cze.z * vz[2]);
+    d.vdov[k] = num / dot3(T, cet);
 }
 
 __global__ void __launch_bounds__(kBlockElem) k_elem_kinematics(const __grid_constant__ Dom d)
