@@ -358,15 +358,29 @@ def main():
         top = max(("elem_force", "node_update", "elem_kinematics", "elem_material"), key=lambda k: per_launch[k])
         achieved = abytes[top] / (per_launch[top] * 1e-3) * 1e-9
         traffic = None
+        fp64 = None
         tf = ROOT / "profiles" / "traffic.json"
         if tf.exists():
             t = json.loads(tf.read_text()).get(precision, {}).get(top)
             if t:
                 traffic = t["bytes_per_elem"] * ne
+                if "fp64_flops_per_unit" in t:
+                    units = nn if top == "node_update" else ne
+                    secs = per_launch[top] * 1e-3
+                    ach = t["fp64_flops_per_unit"] * units / secs * 1e-12
+                    # DADD and DMUL occupy an FP64 issue slot like a DFMA: the
+                    # pipe's utilisation is instructions / (DFMA slots)
+                    inst_rate = t["fp64_inst_per_unit"] * units / secs
+                    slot_rate = fp64_peak * 1e12 / 2.0
+                    fp64 = {"bound": "fp64", "kernel": top, "achieved": ach, "peak": fp64_peak,
+                            "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                            "issue_frac": inst_rate / slot_rate,
+                            "peak_source": "measured FP64 FMA probe (lulesh_probe_fp64_peak)",
+                            "flops_source": "per-unit FP64 work from the ncu capture in profiles/traffic.json"}
         roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                 "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
-                "algorithmic_bytes_per_launch": abytes[top]}
+                "algorithmic_bytes_per_launch": abytes[top], "fp64_issue": fp64}
         total = sum(per_launch.values())
         table = {k: {"ms": per_launch[k], "share": per_launch[k] / total,
                      "gbs": abytes[k] / (per_launch[k] * 1e-3) * 1e-9 if per_launch[k] > 0 else 0.0}
@@ -374,6 +388,7 @@ def main():
         return roof, table, sum(abytes.values()) / ne
 
     mesh = pkg.mesh_build(args.size, pkg.INIT_V2)
+    fp64_peak = pkg.probe_fp64_peak()
 
     # ---- plain FP64: K cycles through the run-loop graph -----------------
     clocks = ClockSampler(local)
@@ -381,7 +396,6 @@ def main():
     value = world * ne * args.steps / (ms * 1e-3) * 1e-6
     ref_metrics = pkg.sedov_metrics(g, mesh)          # state after W + K cycles
     roofline, kernels, cycle_bytes = kernel_table(g, args.precision)
-    fp64_peak = pkg.probe_fp64_peak()
 
     # ---- end to end through the C ABI with host buffers -------------------
     e2e_cycles = args.e2e_cycles or args.steps
@@ -437,8 +451,8 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": config_for(args, ne, nn), "roofline": roofline,
-                "fp64": {"peak_tflops_probe": fp64_peak,
-                         "note": "the FP64 pipe, not HBM, bounds this path: see kernels[*].gbs"},
+                "fp64": {"peak_tflops_probe": fp64_peak, "pipe_rates_per_sm_clk": pkg.probe_pipe_rates(),
+                         "note": "the FP64 pipe, not HBM, bounds this path: see roofline.fp64_issue"},
                 "bytes_per_zone_cycle": cycle_bytes,
                 "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks.summary(), "results": ref_metrics, "split": split,

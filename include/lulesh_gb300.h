@@ -188,6 +188,11 @@ int lulesh_run_profiled(lulesh_ctx *ctx, int max_cycles, int *cycles_done, doubl
  * TFLOP/s (2 flops per FMA), from a register-only kernel. */
 int lulesh_probe_fp64_peak(double *tflops);
 
+/* Issue rates of the current device, in operations per SM per clock at its
+ * maximum clock: rates[0] FP32 FMA, rates[1] FP64 FMA, rates[2] FP64->FP32
+ * conversion (each paired with one FP64 add), rates[3] FP64 division. */
+int lulesh_probe_pipe_rates(double *rates);
+
 /* ---- LagrangeNodal without allocation ---------------------------------
  * No counterpart in the reference: an addition for callers that cannot
  * allocate GPU memory themselves -- code whose device memory is handed out by

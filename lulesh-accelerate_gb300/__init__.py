@@ -122,6 +122,7 @@ _SIGNATURES = {
     "lulesh_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "lulesh_run_profiled": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),
     "lulesh_probe_fp64_peak": (C.c_int, [_dp]),
+    "lulesh_probe_pipe_rates": (C.c_int, [_dp]),
     "lulesh_batch_create": (C.c_int, [C.c_int, _ip, _dp, C.c_int, C.c_int, C.POINTER(Parameters),
                                       C.POINTER(C.c_void_p)]),
     "lulesh_batch_destroy": (None, [C.c_void_p]),
@@ -522,6 +523,14 @@ def probe_fp64_peak() -> float:
     t = C.c_double()
     _check(load_library().lulesh_probe_fp64_peak(C.byref(t)))
     return t.value
+
+
+def probe_pipe_rates() -> dict:
+    """Operations per SM per clock: FP32 FMA, FP64 FMA, FP64->FP32 conversion
+    (paired with an FP64 add), FP64 division."""
+    r = np.zeros(4)
+    _check(load_library().lulesh_probe_pipe_rates(_ptr(r)))
+    return dict(zip(("ffma", "dfma", "d2f_plus_dadd", "ddiv"), r.tolist()))
 
 
 def lulesh(ctx: Lulesh, dom: Domain) -> Domain:

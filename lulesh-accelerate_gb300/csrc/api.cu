@@ -349,8 +349,9 @@ int lulesh_create(int s, int init_mode, int precision, const lulesh_params *para
     } else {
         A(d.f32x, 8 * ne); A(d.f32y, 8 * ne); A(d.f32z, 8 * ne);
         A(d.xs, nn); A(d.ys, nn); A(d.zs, nn); A(d.xds, nn); A(d.yds, nn); A(d.zds, nn);
-        A(d.inv_mass, nn); A(d.gq, 6 * ne);
+        A(d.gq, 6 * ne);
     }
+    A(d.inv_mass, nn);
     A(d.sc, 1); A(ctx->d_active, 1); A(ctx->d_max_cycles, 1);
 #undef A
     d.nodelist = nodelist;
@@ -371,7 +372,8 @@ int lulesh_create(int s, int init_mode, int precision, const lulesh_params *para
         const int k = m.node_elem_corner_list[i];
         slots[i] = (k & 7) * (int)ne + (k >> 3);
     }
-    std::vector<double> zeros(ne, 0.0), ones(ne, 1.0), e(ne, 0.0);
+    std::vector<double> zeros(ne, 0.0), ones(ne, 1.0), e(ne, 0.0), inv_mass(nn);
+    for (size_t i = 0; i < nn; ++i) inv_mass[i] = 1.0 / m.nodal_mass[i];
     e[0] = m.e0;
     cudaStream_t st = ctx->stream;
     auto up = [&](void *dst, const void *src, size_t bytes) {
@@ -383,7 +385,7 @@ int lulesh_create(int s, int init_mode, int precision, const lulesh_params *para
               up(letam, m.letam.data(), ne * 4) && up(letap, m.letap.data(), ne * 4) &&
               up(lzetam, m.lzetam.data(), ne * 4) && up(lzetap, m.lzetap.data(), ne * 4) &&
               up(ebc, m.elem_bc.data(), ne * 4) && up(volo, m.volo.data(), ne * 8) &&
-              up(emass, m.elem_mass.data(), ne * 8) && up(nmass, m.nodal_mass.data(), nn * 8) &&
+              up(emass, m.elem_mass.data(), ne * 8) && up(nmass, m.nodal_mass.data(), nn * 8) && up(d.inv_mass, inv_mass.data(), nn * 8) &&
               up(d.x, m.x.data(), nn * 8) && up(d.y, m.y.data(), nn * 8) && up(d.z, m.z.data(), nn * 8) &&
               up(d.e, e.data(), ne * 8) && up(d.v, ones.data(), ne * 8);
     ok = ok && cudaMemsetAsync(d.xd, 0, nn * 8, st) == cudaSuccess &&
@@ -720,6 +722,48 @@ int lulesh_probe_fp64_peak(double *tflops)
     cudaEventDestroy(b);
     cudaStreamDestroy(st);
     cudaFree(out);
+    return LULESH_OK;
+}
+
+int lulesh_probe_pipe_rates(double *rates)
+{
+    lulesh_ctx *ctx = nullptr;
+    if (!rates) return LULESH_ERR_ARG;
+    int dev = 0, sms = 0, clk_khz = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaDeviceGetAttribute(&clk_khz, cudaDevAttrClockRate, dev));
+    const int threads = 256, blocks = sms * 8;
+    float *out = nullptr;
+    CK(cudaMalloc(&out, sizeof(float) * threads * blocks));
+    double *dout = nullptr;
+    CK(cudaMalloc(&dout, sizeof(double)));
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    // ops per thread of each probe: FFMA, DFMA, D2F (+DADD), DDIV
+    const int iters[4] = {4096, 1024, 1024, 64};
+    const double ops[4] = {8.0 * 4096, 8.0 * 1024, 8.0 * 1024, 4.0 * 64};
+    for (int w = 0; w < 4; ++w) {
+        for (int rep = 0; rep < 2; ++rep) {     // the first launch warms up
+            CK(cudaEventRecord(a, st));
+            if (w == 1) launch_fp64_probe(dout, blocks, threads, iters[w], st);
+            else launch_rate_probe(w == 0 ? 0 : (w == 2 ? 1 : 2), out, blocks, threads, iters[w], st);
+            CK(cudaEventRecord(b, st));
+        }
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        // operations per SM per clock at the nominal maximum clock
+        rates[w] = ops[w] * threads * blocks / (ms * 1e-3) / ((double)clk_khz * 1e3) / sms;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaStreamDestroy(st);
+    cudaFree(out);
+    cudaFree(dout);
     return LULESH_OK;
 }
 

@@ -63,6 +63,10 @@ __device__ __forceinline__ void time_increment(DevScalars *sc, const lulesh_para
     ++sc->cycle;
 }
 
+// 1/x, correctly rounded in both precisions (the bits of a division).
+__device__ __forceinline__ double recip(double x) { return __drcp_rn(x); }
+__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
+
 // One direction of the monotonic limiter (:2198-2228).
 template <typename T>
 __device__ __forceinline__ T limiter_phi(const T *__restrict__ delv, int i, int bm, int bp,
@@ -71,7 +75,7 @@ __device__ __forceinline__ T limiter_phi(const T *__restrict__ delv, int i, int 
 {
     const T ptiny = T(1.e-36);
     const T own = delv[i];
-    const T norm = T(1.) / (own + ptiny);
+    const T norm = recip(own + ptiny);
     T delvm = T(0.0), delvp = T(0.0);
     if (bm == 0) delvm = delv[lm];
     else if (bm == m_symm) delvm = own;
@@ -142,9 +146,10 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
     // EvalEOSForElems + CalcEnergyForElems (:2415-2701); work == 0
     const double delvc = d.delv[k], e_old = d.e[k];
     double p_old = d.p[k];
-    double compression = 1. / vnewc - 1.;
+    // __drcp_rn is the correctly rounded reciprocal: the bits of 1. / x
+    double compression = __drcp_rn(vnewc) - 1.;
     const double vchalf = vnewc - delvc * .5;
-    double comp_half = 1. / vchalf - 1.;
+    double comp_half = __drcp_rn(vchalf) - 1.;
     // vhalf = 1 / (1 + comp_half) (:2460), which is vchalf, vnewc or 1 in the
     // three cases below; taken directly instead of through two divisions
     double vhalf = vchalf;

@@ -28,6 +28,7 @@ constexpr int kRunCycleLimit = 1 << 26;
 constexpr int kTimedKernels = 6;   // time increment, force, node, kinematics, material, finalize
 void launch_cycle_timed(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTimedKernels + 1]);
 void launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t st);
+void launch_rate_probe(int which, float *out, int blocks, int threads, int iters, cudaStream_t st);
 
 // Split-precision path (step_split.cu).
 void launch_split_sync(const Dom &d, cudaStream_t st);

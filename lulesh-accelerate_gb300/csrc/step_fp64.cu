@@ -173,11 +173,20 @@ __device__ __forceinline__ void node_update_fp64(const Dom &d, int n, const DevS
         d.fz[n] = fz;
     }
     const double dt = sc->deltatime, u_cut = d.prm.u_cut;
-    const double m = __ldg(d.nodal_mass + n);
     const unsigned bc = __ldg(d.node_bc + n);
-    const double ax = (bc & 1) ? 0.0 : fx / m;
-    const double ay = (bc & 2) ? 0.0 : fy / m;
-    const double az = (bc & 4) ? 0.0 : fz / m;
+    double ax, ay, az;
+    if (d.inv_mass) {
+        // f * (1/m) with the reciprocal precomputed: within an ulp of f / m
+        const double im = __ldg(d.inv_mass + n);
+        ax = (bc & 1) ? 0.0 : fx * im;
+        ay = (bc & 2) ? 0.0 : fy * im;
+        az = (bc & 4) ? 0.0 : fz * im;
+    } else {
+        const double m = __ldg(d.nodal_mass + n);
+        ax = (bc & 1) ? 0.0 : fx / m;
+        ay = (bc & 2) ? 0.0 : fy / m;
+        az = (bc & 4) ? 0.0 : fz / m;
+    }
     double t;
     t = d.xd[n] + ax * dt; if (fabs(t) < u_cut) t = 0.0; d.xd[n] = t; d.x[n] += t * dt;
     t = d.yd[n] + ay * dt; if (fabs(t) < u_cut) t = 0.0; d.yd[n] = t; d.y[n] += t * dt;
@@ -237,7 +246,7 @@ __device__ __forceinline__ void elem_kinematics_fp64(const Dom &d, int k, DevSca
     {
         const double ptiny = 1.e-36;
         const double vol = volo * rel;
-        const double norm = 1.0 / (vol + ptiny);
+        const double norm = __drcp_rn(vol + ptiny);
         const double vscale = 0.015625 * norm;           // (1/16) (1/4) norm
         const V3<double> Az = cross3(M1, M2), Ax = cross3(M2, M3), Ae = cross3(M3, M1);
         d.delx_zeta[k] = vol * rsqrt(0.00390625 * dot3(Az, Az) + ptiny);
@@ -468,6 +477,62 @@ __global__ void k_fp64_probe(double *out, int iters, double a, double b)
 void launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t st)
 {
     k_fp64_probe<<<blocks, threads, 0, st>>>(out, iters, 0.999999, 1e-7);
+}
+
+// Issue-rate probes for the design notes: 8 independent chains per thread
+// of one operation; each thread writes one value (keeps the chains live).
+__global__ void k_probe_ffma(float *out, int iters, float a, float b)
+{
+    float r[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) r[j] = threadIdx.x * 1e-3f + j;
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) r[j] = fmaf(r[j], a, b);
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += r[j];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// double -> float conversions (each iteration: one conversion, one DADD).
+__global__ void k_probe_d2f(float *out, int iters, double a)
+{
+    double r[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) r[j] = threadIdx.x * 1e-3 + j;
+    float acc = 0.f;
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            acc += __double2float_rn(r[j]);
+            r[j] += a;
+        }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+// correctly rounded FP64 division
+__global__ void k_probe_ddiv(float *out, int iters, double a)
+{
+    double r[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) r[j] = threadIdx.x * 1e-3 + j + 1.0;
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) r[j] = a / r[j];
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) s += r[j];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = (float)s;
+}
+
+void launch_rate_probe(int which, float *out, int blocks, int threads, int iters, cudaStream_t st)
+{
+    switch (which) {
+    case 0: k_probe_ffma<<<blocks, threads, 0, st>>>(out, iters, 0.9999f, 1e-7f); break;
+    case 1: k_probe_d2f<<<blocks, threads, 0, st>>>(out, iters, 1e-9); break;
+    default: k_probe_ddiv<<<blocks, threads, 0, st>>>(out, iters, 1.2345); break;
+    }
 }
 
 // ---------------------------------------------------------------------
