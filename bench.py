@@ -242,6 +242,25 @@ def batch_legs(pkg, torch, args, barrier, max_over_ranks) -> dict:
     return out
 
 
+def reduce_max(x: float, world: int) -> float:
+    """Largest value over the ranks (the job lasts as long as its slowest rank)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, ms_per_rank: float, world: int) -> float:
+    """Million units per second of the whole job: every rank ran one replica
+    of the same work (weak scaling), timed by the slowest rank."""
+    return world * units_per_rank / (reduce_max(ms_per_rank, world) * 1e-3) * 1e-6
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -323,11 +342,7 @@ def main():
             torch.cuda.synchronize()
 
     def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(x, world)
 
     def timed(ctx, steps, clocks=None):
         """K cycles after W warm-up cycles; device ms on the library's stream."""
@@ -392,7 +407,7 @@ def main():
 
     # ---- plain FP64: K cycles through the run-loop graph -----------------
     clocks = ClockSampler(local)
-    ms, launches = timed(g, args.steps, clocks)
+    ms, launches = timed(g, args.steps, clocks)       # already the slowest rank's time
     value = world * ne * args.steps / (ms * 1e-3) * 1e-6
     ref_metrics = pkg.sedov_metrics(g, mesh)          # state after W + K cycles
     roofline, kernels, cycle_bytes = kernel_table(g, args.precision)

@@ -18,6 +18,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "liblulesh_gb300.so"
+DRIVER = PKG / "lulesh_gb300_main"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
@@ -47,8 +48,9 @@ def _compile(src: str, verbose: bool) -> Path:
 
 def build(verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    deps = sorted(CSRC.glob("*")) + [PKG.parent / "include" / "lulesh_gb300.h", Path(__file__)]
-    if LIB.exists() and not verbose:
+    deps = sorted(CSRC.glob("*")) + sorted((PKG / "driver").glob("*")) + [PKG.parent / "include" / "lulesh_gb300.h",
+                                                                         Path(__file__)]
+    if LIB.exists() and DRIVER.exists() and not verbose:
         newest = max(p.stat().st_mtime for p in deps)
         if LIB.stat().st_mtime > newest:
             return LIB
@@ -60,6 +62,14 @@ def build(verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # the C host (driver/lulesh_gb300_main.c): links the library through its
+    # C header only, as the reference's C driver would
+    cc = shutil.which("gcc") or "cc"
+    cmd = [cc, "-O2", "-std=c99", "-I", str(PKG.parent / "include"), str(PKG / "driver" / "lulesh_gb300_main.c"),
+           "-L", str(PKG), "-llulesh_gb300", f"-Wl,-rpath,{PKG}", "-o", str(DRIVER)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

@@ -59,20 +59,29 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
     walsh8(z, mz);
     const V3<double> M1 = mode(mx, my, mz, 0), M2 = mode(mx, my, mz, 1), M3 = mode(mx, my, mz, 2);
 
+    const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
+    double dvdx[8], dvdy[8], dvdz[8];
+    V3<double> pf[4];
+    force_geometry64(M1, M2, M3, M4, M5, M6, dvdx, dvdy, dvdz, pf);   // 64 x dV/dx, 64 x normals
+
     // IntegrateStressForElems (LULESH-OMP.cc:853-903): sig = -p - q and the
-    // corner force -sig * (area-weighted node normal).  The Jacobian volume
-    // it checks is 8 t.(c x a) = M2.(M3 x M1) / 64; only its sign matters.
+    // corner force -sig * (area-weighted node normal); corners 4..7 carry
+    // the negated forces of corners 2, 3, 0, 1.  The Jacobian volume it
+    // checks is 8 t.(c x a) = M2.(M3 x M1) / 64; only its sign matters.
     {
-        const double determ64 = dot3(M2, cross3(M3, M1));
-        double pf[3][8];
-        node_normals8(pf, x, y, z);                      // 8 x the normals
-        const double sig8 = 0.125 * (-d.p[k] - d.q[k]);
+        const double sig64 = (1.0 / 64.0) * (-d.p[k] - d.q[k]);
+        const int neg_of[4] = {6, 7, 4, 5};
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            d.fsx[c * ne + k] = -(sig8 * pf[0][c]);
-            d.fsy[c * ne + k] = -(sig8 * pf[1][c]);
-            d.fsz[c * ne + k] = -(sig8 * pf[2][c]);
+        for (int c = 0; c < 4; ++c) {
+            const double fx = -(sig64 * pf[c].x), fy = -(sig64 * pf[c].y), fz = -(sig64 * pf[c].z);
+            d.fsx[c * ne + k] = fx;
+            d.fsy[c * ne + k] = fy;
+            d.fsz[c * ne + k] = fz;
+            d.fsx[neg_of[c] * ne + k] = -fx;
+            d.fsy[neg_of[c] * ne + k] = -fy;
+            d.fsz[neg_of[c] * ne + k] = -fz;
         }
+        const double determ64 = dot3(M2, cross3(M3, M1));
         if (determ64 <= 0.0) flag_error(sc, ERR_K1_DETERM, k);
     }
 
@@ -94,15 +103,12 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
 
     // CalcFBHourglassForceForElems (:1291-1473): hourgam = gamma -
     // volinv * (dV/dx . hourmod), with hourmod the gamma projections of the
-    // coordinates (modes M6, M5, M4, M7) and dV/dx from the modes.
+    // coordinates (modes M6, M5, M4, M7).
     const double r = rcbrt(determ);                       // determ^(-1/3)
-    const double volinv64 = (r * r * r) * (1.0 / 64.0);   // the 1/64 of volume_derivative64
+    const double volinv64 = (r * r * r) * (1.0 / 64.0);   // the 1/64 of the derivative
     double hg[8][4];
     {
-        const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
         const V3<double> M7 = mode(mx, my, mz, 6);
-        double dvdx[8], dvdy[8], dvdz[8];
-        volume_derivative64(M1, M2, M3, M4, M5, M6, dvdx, dvdy, dvdz);
         const V3<double> H[4] = {M6, M5, M4, M7};
         const double gam[4][8] = {
             { 1.,  1., -1., -1., -1., -1.,  1.,  1.},
