@@ -107,6 +107,54 @@ int lulesh_create(int s, int init_mode, int precision, const lulesh_params *para
                   lulesh_ctx **out);
 void lulesh_destroy(lulesh_ctx *ctx);
 
+/* ---- unstructured meshes ----------------------------------------------
+ * An arbitrary hexahedral mesh, as the reference's unstructured reader takes
+ * it (reference/CUDA/lulesh-kepler-singlegpu/lulesh.cu:733-923, the "-u
+ * file.lmesh" mode of its main(), :3324-3328, :3479-3494).  All arrays are
+ * host memory, read during the call only:
+ *   x, y, z [num_node]          initial node coordinates;
+ *   nodelist [8*num_elem]       the 8 nodes of each element, element-major,
+ *                               corners in the reference's order;
+ *   lxim..lzetap [num_elem]     face neighbours (xi-, xi+, eta-, eta+, zeta-,
+ *                               zeta+), the element itself on a boundary face;
+ *   symm_x/y/z [num_symm_*]     nodes on the x, y, z symmetry planes, whose
+ *                               x, y, z acceleration the step zeroes;
+ *   free_surf [num_free_surf]   free-surface nodes.
+ * Set-up follows the reader: a face whose four corners all lie in the union
+ * of the symmetry sets, then a face whose four corners all lie in the free-
+ * surface set, is flagged SYMM for the monotonic-Q limiter; the initial
+ * energy 3.948746e7 goes to the origin element (the first one flagged SYMM
+ * on exactly its xi-, eta- and zeta- faces by the symmetry pass; element 0 if
+ * there is none) and the first time step is 1e-7 (LULESH 1.0).  Node-to-
+ * corner lists, reference volumes and masses are built as on the cube. */
+typedef struct lulesh_unstructured_mesh {
+    long num_elem, num_node;
+    const double *x, *y, *z;
+    const int *nodelist;
+    const int *lxim, *lxip, *letam, *letap, *lzetam, *lzetap;
+    const int *symm_x, *symm_y, *symm_z, *free_surf;
+    long num_symm_x, num_symm_y, num_symm_z, num_free_surf;
+} lulesh_unstructured_mesh;
+
+/* A context for an unstructured mesh.  LULESH_ERR_ARG (nothing allocated)
+ * for an empty mesh, more than 2^28-1 elements, an index out of range, or a
+ * node that belongs to no element. */
+int lulesh_create_unstructured(const lulesh_unstructured_mesh *mesh, int precision,
+                               const lulesh_params *params, lulesh_ctx **out);
+
+/* Read a .lmesh text file (numElem numNode; numNode coordinate triples; 8
+ * node indices per element; 6 face neighbours per element; then the
+ * symmetry X, Y, Z and free-surface node sets, each a count followed by its
+ * node indices) and create a context for it.  Where the reference exits
+ * with LFileError on a file it cannot read, this returns LULESH_ERR_ARG. */
+int lulesh_create_lmesh(const char *path, int precision, const lulesh_params *params,
+                        lulesh_ctx **out);
+
+/* The element holding the initial energy (0 on the cube); its energy is what
+ * lulesh_origin_energy reports (the reference's domain->octantCorner,
+ * lulesh.cu:3540-3542). */
+int lulesh_origin_element(lulesh_ctx *ctx, long *elem);
+
 /* Message of the last failing call on this context (static storage when ctx
  * is NULL). */
 const char *lulesh_last_error(const lulesh_ctx *ctx);
@@ -159,12 +207,14 @@ int lulesh_lagrange_leapfrog(lulesh_ctx *ctx);     /* LagrangeLeapFrog   LULESH-
  * inside one CUDA graph; the host does not wait per cycle. */
 int lulesh_run(lulesh_ctx *ctx, int max_cycles, int *cycles_done);
 
-/* Result checks of LULESH-OMP.cc:3197-3223 / src/Main.hs:132-156. */
+/* Result checks of LULESH-OMP.cc:3197-3223 / src/Main.hs:132-156.  The
+ * plane-0 symmetry test needs the cube: LULESH_ERR_ARG on an unstructured
+ * mesh. */
 int lulesh_origin_energy(lulesh_ctx *ctx, double *e0);
 int lulesh_symmetry(lulesh_ctx *ctx, double *max_abs_diff, double *total_abs_diff,
                     double *max_rel_diff);
 
-/* Sizes of this context's mesh. */
+/* Sizes of this context's mesh (s = 0 for an unstructured mesh). */
 int lulesh_sizes(lulesh_ctx *ctx, int *s, long *num_elem, long *num_node);
 
 /* The context's cudaStream_t (as void*), for callers that time or order

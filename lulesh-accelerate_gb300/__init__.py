@@ -93,11 +93,29 @@ class MeshView(C.Structure):
                 ("e0", C.c_double), ("dt0", C.c_double)]
 
 
+class UnstructuredMesh(C.Structure):
+    """``lulesh_unstructured_mesh``: host arrays of an arbitrary hex mesh."""
+
+    _fields_ = [("num_elem", C.c_long), ("num_node", C.c_long),
+                ("x", _dp), ("y", _dp), ("z", _dp), ("nodelist", _ip)] + \
+               [(n, _ip) for n in ("lxim", "lxip", "letam", "letap", "lzetam", "lzetap",
+                                   "symm_x", "symm_y", "symm_z", "free_surf")] + \
+               [(n, C.c_long) for n in ("num_symm_x", "num_symm_y", "num_symm_z", "num_free_surf")]
+
+
+MESH_ARRAYS = ("x", "y", "z", "nodelist", "lxim", "lxip", "letam", "letap", "lzetam", "lzetap",
+               "symm_x", "symm_y", "symm_z", "free_surf")
+
+
 _SIGNATURES = {
     "lulesh_default_params": (None, [C.POINTER(Parameters)]),
     "lulesh_mesh_sizes": (C.c_int, [C.c_int, C.POINTER(C.c_long), C.POINTER(C.c_long)]),
     "lulesh_mesh_build": (C.c_int, [C.c_int, C.c_int, C.POINTER(MeshView)]),
     "lulesh_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(Parameters), C.POINTER(C.c_void_p)]),
+    "lulesh_create_unstructured": (C.c_int, [C.POINTER(UnstructuredMesh), C.c_int, C.POINTER(Parameters),
+                                             C.POINTER(C.c_void_p)]),
+    "lulesh_create_lmesh": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(Parameters), C.POINTER(C.c_void_p)]),
+    "lulesh_origin_element": (C.c_int, [C.c_void_p, C.POINTER(C.c_long)]),
     "lulesh_destroy": (None, [C.c_void_p]),
     "lulesh_last_error": (C.c_char_p, [C.c_void_p]),
     "lulesh_upload_domain": (C.c_int, [C.c_void_p] + [_dp] * 11 + [C.c_double, C.c_double]),
@@ -253,15 +271,55 @@ class Lulesh:
     """
 
     def __init__(self, s: int, init: int = INIT_V2, precision: int = FP64,
-                 params: Parameters | None = None):
+                 params: Parameters | None = None, *, _handle: C.c_void_p | None = None):
         lib = load_library()
-        h = C.c_void_p()
-        rc = lib.lulesh_create(s, init, precision, C.byref(params) if params is not None else None,
-                               C.byref(h))
-        _check(rc)
+        if _handle is None:
+            h = C.c_void_p()
+            rc = lib.lulesh_create(s, init, precision, C.byref(params) if params is not None else None,
+                                   C.byref(h))
+            _check(rc)
+        else:
+            h = _handle
         self._h = h
-        self.s = s
-        self.num_elem, self.num_node = mesh_sizes(s)
+        es, ne, nn = C.c_int(), C.c_long(), C.c_long()
+        _check(lib.lulesh_sizes(h, C.byref(es), C.byref(ne), C.byref(nn)), h)
+        self.s = es.value
+        self.num_elem, self.num_node = ne.value, nn.value
+
+    @classmethod
+    def from_mesh(cls, mesh: dict, precision: int = FP64, params: Parameters | None = None) -> "Lulesh":
+        """An unstructured problem from host arrays (keys of ``MESH_ARRAYS``;
+        the reference's unstructured set-up, lulesh.cu:733-923)."""
+        keep = {}
+        m = UnstructuredMesh(num_elem=len(mesh["nodelist"]) // 8, num_node=len(mesh["x"]))
+        for k in MESH_ARRAYS:
+            dt = np.float64 if k in ("x", "y", "z") else np.int32
+            a = np.ascontiguousarray(mesh[k], dtype=dt)
+            keep[k] = a
+            setattr(m, k, _ptr(a, C.c_double if dt is np.float64 else C.c_int))
+        m.num_symm_x, m.num_symm_y, m.num_symm_z = (len(keep[k]) for k in ("symm_x", "symm_y", "symm_z"))
+        m.num_free_surf = len(keep["free_surf"])
+        h = C.c_void_p()
+        rc = load_library().lulesh_create_unstructured(
+            C.byref(m), precision, C.byref(params) if params is not None else None, C.byref(h))
+        _check(rc)
+        return cls(0, _handle=h)
+
+    @classmethod
+    def from_lmesh(cls, path, precision: int = FP64, params: Parameters | None = None) -> "Lulesh":
+        """An unstructured problem read from a .lmesh text file by the library."""
+        h = C.c_void_p()
+        rc = load_library().lulesh_create_lmesh(
+            os.fsencode(str(path)), precision, C.byref(params) if params is not None else None, C.byref(h))
+        _check(rc)
+        return cls(0, _handle=h)
+
+    @property
+    def origin(self) -> int:
+        """Element holding the initial energy (the reference's octantCorner)."""
+        e = C.c_long()
+        _check(load_library().lulesh_origin_element(self._h, C.byref(e)), self._h)
+        return e.value
 
     # lifetime -----------------------------------------------------------
     def close(self):
@@ -486,7 +544,8 @@ def ensemble(seed: int, n: int, lo: int, hi: int, extra_sizes=()) -> tuple[np.nd
 def sedov_metrics(ctx: "Lulesh", mesh: dict | None = None) -> dict:
     """Whole-problem results of a Sedov state, for comparing precisions.
 
-    * ``origin_energy``: e of element 0 (the reference's printed result);
+    * ``origin_energy``: e of the origin element (the reference's printed
+      result; element 0 on the cube);
     * ``total_energy``: internal plus kinetic energy,
       sum(e * elemMass) + sum(0.5 * nodalMass * |v|^2);
     * ``max_velocity``: largest nodal speed |v|;
@@ -507,7 +566,7 @@ def sedov_metrics(ctx: "Lulesh", mesh: dict | None = None) -> dict:
     r = np.sqrt(cx * cx + cy * cy + cz * cz)
     w = q * m["elem_mass"]
     return {
-        "origin_energy": float(e[0]),
+        "origin_energy": float(e[ctx.origin]),
         "total_energy": float(np.sum(e * m["elem_mass"]) + 0.5 * np.sum(m["nodal_mass"] * speed2)),
         "max_velocity": float(np.sqrt(np.max(speed2))),
         "shock_radius": float(np.sum(r * w) / np.sum(w)) if np.sum(w) > 0 else 0.0,

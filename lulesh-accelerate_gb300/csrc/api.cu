@@ -30,6 +30,7 @@ struct lulesh_ctx {
     cudaGraphExec_t chunk_exec = nullptr;
     int status = LULESH_OK;          // sticky step error
     long long launches = 0;
+    long origin = 0;                 // element holding the initial energy
     std::string err;
 };
 
@@ -291,22 +292,21 @@ void lulesh_destroy(lulesh_ctx *ctx)
     delete ctx;
 }
 
-int lulesh_create(int s, int init_mode, int precision, const lulesh_params *params, lulesh_ctx **out)
+}  // extern "C"
+
+namespace {
+
+// A context for a built host mesh: device arrays, initial state, stream.
+int create_from_mesh(const HostMesh &m, int precision, const lulesh_params *params, lulesh_ctx **out)
 {
-    lulesh_ctx *ctx = nullptr;
-    if (!out || s < 1 || s > kMaxEdge) return fail(nullptr, LULESH_ERR_ARG, "lulesh_create: bad size or output pointer");
-    if (init_mode != LULESH_INIT_V1 && init_mode != LULESH_INIT_V2)
-        return fail(nullptr, LULESH_ERR_ARG, "lulesh_create: init_mode must be LULESH_INIT_V1 or LULESH_INIT_V2");
-    if (precision != LULESH_PRECISION_FP64 && precision != LULESH_PRECISION_SPLIT)
-        return fail(nullptr, LULESH_ERR_ARG, "lulesh_create: unknown precision");
+    const int s = m.s;
     *out = nullptr;
-    ctx = new lulesh_ctx;
+    lulesh_ctx *ctx = new lulesh_ctx;
     int rc = LULESH_OK;
     auto bail = [&](int code) { g_err = ctx->err; lulesh_destroy(ctx); return code; };
 
-    HostMesh m;
-    m.build(s, init_mode);
     ctx->s = s;
+    ctx->origin = m.origin;
     ctx->ne = m.ne;
     ctx->nn = m.nn;
     ctx->precision = precision;
@@ -374,7 +374,7 @@ int lulesh_create(int s, int init_mode, int precision, const lulesh_params *para
     }
     std::vector<double> zeros(ne, 0.0), ones(ne, 1.0), e(ne, 0.0), inv_mass(nn);
     for (size_t i = 0; i < nn; ++i) inv_mass[i] = 1.0 / m.nodal_mass[i];
-    e[0] = m.e0;
+    e[m.origin] = m.e0;
     cudaStream_t st = ctx->stream;
     auto up = [&](void *dst, const void *src, size_t bytes) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st) == cudaSuccess;
@@ -417,6 +417,58 @@ int lulesh_create(int s, int init_mode, int precision, const lulesh_params *para
         return bail(LULESH_ERR_CUDA);
     }
     *out = ctx;
+    return LULESH_OK;
+}
+
+int check_precision(int precision, const char *who)
+{
+    if (precision != LULESH_PRECISION_FP64 && precision != LULESH_PRECISION_SPLIT)
+        return fail(nullptr, LULESH_ERR_ARG, std::string(who) + ": unknown precision");
+    return LULESH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lulesh_create(int s, int init_mode, int precision, const lulesh_params *params, lulesh_ctx **out)
+{
+    if (!out || s < 1 || s > kMaxEdge) return fail(nullptr, LULESH_ERR_ARG, "lulesh_create: bad size or output pointer");
+    if (init_mode != LULESH_INIT_V1 && init_mode != LULESH_INIT_V2)
+        return fail(nullptr, LULESH_ERR_ARG, "lulesh_create: init_mode must be LULESH_INIT_V1 or LULESH_INIT_V2");
+    if (int rc = check_precision(precision, "lulesh_create")) return rc;
+    HostMesh m;
+    m.build(s, init_mode);
+    return create_from_mesh(m, precision, params, out);
+}
+
+int lulesh_create_unstructured(const lulesh_unstructured_mesh *mesh, int precision, const lulesh_params *params,
+                               lulesh_ctx **out)
+{
+    if (!out || !mesh) return fail(nullptr, LULESH_ERR_ARG, "lulesh_create_unstructured: NULL argument");
+    *out = nullptr;
+    if (int rc = check_precision(precision, "lulesh_create_unstructured")) return rc;
+    HostMesh m;
+    std::string err;
+    if (m.build_unstructured(*mesh, &err) != LULESH_OK) return fail(nullptr, LULESH_ERR_ARG, err);
+    return create_from_mesh(m, precision, params, out);
+}
+
+int lulesh_create_lmesh(const char *path, int precision, const lulesh_params *params, lulesh_ctx **out)
+{
+    if (!out) return fail(nullptr, LULESH_ERR_ARG, "lulesh_create_lmesh: NULL output pointer");
+    *out = nullptr;
+    if (int rc = check_precision(precision, "lulesh_create_lmesh")) return rc;
+    LmeshFile f;
+    std::string err;
+    if (f.read(path, &err) != LULESH_OK) return fail(nullptr, LULESH_ERR_ARG, err);
+    return lulesh_create_unstructured(&f.view, precision, params, out);
+}
+
+int lulesh_origin_element(lulesh_ctx *ctx, long *elem)
+{
+    if (!ctx || !elem) return LULESH_ERR_ARG;
+    *elem = ctx->origin;
     return LULESH_OK;
 }
 
@@ -770,7 +822,7 @@ int lulesh_probe_pipe_rates(double *rates)
 int lulesh_origin_energy(lulesh_ctx *ctx, double *e0)
 {
     if (!ctx || !e0) return LULESH_ERR_ARG;
-    CK(cudaMemcpyAsync(ctx->h_sc, ctx->dom.e, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->h_sc, ctx->dom.e + ctx->origin, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     memcpy(e0, ctx->h_sc, sizeof(double));
     return LULESH_OK;
@@ -780,6 +832,7 @@ int lulesh_symmetry(lulesh_ctx *ctx, double *max_abs_diff, double *total_abs_dif
 {
     if (!ctx) return LULESH_ERR_ARG;
     const int s = ctx->s;
+    if (s < 1) return fail(ctx, LULESH_ERR_ARG, "lulesh_symmetry: the plane-0 test needs the cube mesh");
     std::vector<double> plane((size_t)s * s);
     CK(cudaMemcpyAsync(plane.data(), ctx->dom.e, plane.size() * sizeof(double), cudaMemcpyDeviceToHost,
                        ctx->stream));

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <vector_types.h>
+#include <string>
 #include <vector>
 
 namespace lulesh {
@@ -56,7 +57,21 @@ struct HostMesh {
     std::vector<int> lxim, lxip, letam, letap, lzetam, lzetap, elem_bc;
     std::vector<unsigned char> node_bc;  // bit0 x=0, bit1 y=0, bit2 z=0 plane
     double e0 = 0.0, dt0 = 0.0;
+    long origin = 0;                     // element holding e0
     void build(int s, int init_mode);
+    // LULESH_OK, or LULESH_ERR_ARG with a message in *err
+    int build_unstructured(const lulesh_unstructured_mesh &u, std::string *err);
+
+  private:
+    void derive();                       // corner lists, volumes, masses
+};
+
+// The numbers of a .lmesh file; the arrays back a lulesh_unstructured_mesh.
+struct LmeshFile {
+    lulesh_unstructured_mesh view{};
+    std::vector<double> x, y, z;
+    std::vector<int> nodelist, nb[6], sets[4];
+    int read(const char *path, std::string *err);
 };
 
 double host_elem_volume(const double x[8], const double y[8], const double z[8]);

@@ -1,14 +1,20 @@
-// mesh.cpp -- host construction of the Sedov cube.
+// mesh.cpp -- host construction of the Sedov problem.
 //
 // Builds what the reference's main() builds before its time loop
 // (reference/C/LULESH-OMP.cc:2960-3171): coordinates, hexahedron
 // connectivity, node-to-corner lists (AllocateNodeElemIndexes :209-268),
 // reference volumes and masses, face neighbours, boundary-condition bits and
-// the initial energy / time step.  Compiled with -ffp-contract=off so that
-// the floating-point results are the reference's on every host architecture.
+// the initial energy / time step -- on the s^3 cube, or on an unstructured
+// mesh as the reference's unstructured reader sets it up
+// (reference/CUDA/lulesh-kepler-singlegpu/lulesh.cu:733-923).  Compiled with
+// -ffp-contract=off so that the floating-point results are the reference's
+// on every host architecture.
 #include "lulesh_internal.h"
 
+#include <cerrno>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -70,6 +76,41 @@ void default_params(lulesh_params *p)
     p->refdens = 1.0;
 }
 
+// Node-to-corner lists in (element, corner) order, reference volumes and the
+// element and nodal masses of a filled-in nodelist.
+void HostMesh::derive()
+{
+    // node -> corner lists in (element, corner) order: a counting sort.
+    node_elem_count.assign(nn, 0);
+    node_elem_start.assign(nn, 0);
+    node_elem_corner_list.assign(8 * ne, 0);
+    for (long i = 0; i < 8 * ne; ++i) node_elem_count[nodelist[i]]++;
+    for (long i = 1; i < nn; ++i) node_elem_start[i] = node_elem_start[i - 1] + node_elem_count[i - 1];
+    std::vector<int> fill(nn, 0);
+    for (long i = 0; i < ne; ++i)
+        for (int j = 0; j < 8; ++j) {
+            const int m = nodelist[8 * i + j];
+            node_elem_corner_list[node_elem_start[m] + fill[m]++] = int(8 * i + j);
+        }
+
+    volo.assign(ne, 0.0);
+    elem_mass.assign(ne, 0.0);
+    nodal_mass.assign(nn, 0.0);
+    for (long i = 0; i < ne; ++i) {
+        double xl[8], yl[8], zl[8];
+        for (int k = 0; k < 8; ++k) {
+            const int g = nodelist[8 * i + k];
+            xl[k] = x[g];
+            yl[k] = y[g];
+            zl[k] = z[g];
+        }
+        const double vol = host_elem_volume(xl, yl, zl);
+        volo[i] = vol;
+        elem_mass[i] = vol;
+        for (int k = 0; k < 8; ++k) nodal_mass[nodelist[8 * i + k]] += vol / 8.0;
+    }
+}
+
 void HostMesh::build(int s_, int init_mode)
 {
     s = s_;
@@ -107,36 +148,9 @@ void HostMesh::build(int s_, int init_mode)
                 l[7] = n0 + en * en + en;
             }
 
-    // node -> corner lists in (element, corner) order: a counting sort.
-    node_elem_count.assign(nn, 0);
-    node_elem_start.assign(nn, 0);
-    node_elem_corner_list.assign(8 * ne, 0);
-    for (long i = 0; i < 8 * ne; ++i) node_elem_count[nodelist[i]]++;
-    for (long i = 1; i < nn; ++i) node_elem_start[i] = node_elem_start[i - 1] + node_elem_count[i - 1];
-    std::vector<int> fill(nn, 0);
-    for (long i = 0; i < ne; ++i)
-        for (int j = 0; j < 8; ++j) {
-            const int m = nodelist[8 * i + j];
-            node_elem_corner_list[node_elem_start[m] + fill[m]++] = int(8 * i + j);
-        }
+    derive();
 
-    volo.assign(ne, 0.0);
-    elem_mass.assign(ne, 0.0);
-    nodal_mass.assign(nn, 0.0);
-    for (long i = 0; i < ne; ++i) {
-        double xl[8], yl[8], zl[8];
-        for (int k = 0; k < 8; ++k) {
-            const int g = nodelist[8 * i + k];
-            xl[k] = x[g];
-            yl[k] = y[g];
-            zl[k] = z[g];
-        }
-        const double vol = host_elem_volume(xl, yl, zl);
-        volo[i] = vol;
-        elem_mass[i] = vol;
-        for (int k = 0; k < 8; ++k) nodal_mass[nodelist[8 * i + k]] += vol / 8.0;
-    }
-
+    origin = 0;
     if (init_mode == LULESH_INIT_V2) {
         // lulesh-2.0.3/lulesh-init.cc:171-182
         const double ebase = 3.948746e+7;
@@ -183,6 +197,178 @@ void HostMesh::build(int s_, int init_mode)
             elem_bc[rinc + j + ne - s2] |= BC_ZETA_P_FREE;
         }
     }
+}
+
+// Face flags of the reference's unstructured reader (lulesh.cu:852-920): a
+// face whose four corners all carry the mark is flagged SYMM -- in the
+// free-surface pass as well.  Corner bits 0-3 form the zeta- face, 4-7
+// zeta+, {0,1,4,5} eta-, {2,3,6,7} eta+, {0,3,4,7} xi-, {1,2,5,6} xi+.
+static void flag_faces(const std::vector<int> &nodelist, const std::vector<unsigned char> &mark,
+                       std::vector<int> &elem_bc)
+{
+    const long ne = (long)elem_bc.size();
+    for (long k = 0; k < ne; ++k) {
+        int mask = 0;
+        for (int c = 0; c < 8; ++c) mask |= (mark[nodelist[8 * k + c]] ? 1 : 0) << c;
+        int &bc = elem_bc[k];
+        if ((mask & 0x0f) == 0x0f) bc |= BC_ZETA_M_SYMM;
+        if ((mask & 0xf0) == 0xf0) bc |= BC_ZETA_P_SYMM;
+        if ((mask & 0x33) == 0x33) bc |= BC_ETA_M_SYMM;
+        if ((mask & 0xcc) == 0xcc) bc |= BC_ETA_P_SYMM;
+        if ((mask & 0x99) == 0x99) bc |= BC_XI_M_SYMM;
+        if ((mask & 0x66) == 0x66) bc |= BC_XI_P_SYMM;
+    }
+}
+
+int HostMesh::build_unstructured(const lulesh_unstructured_mesh &u, std::string *err)
+{
+    auto bad = [&](const std::string &m) {
+        if (err) *err = "unstructured mesh: " + m;
+        return LULESH_ERR_ARG;
+    };
+    if (u.num_elem < 1 || u.num_node < 1) return bad("empty mesh");
+    if (u.num_elem > (1L << 28) - 1 || u.num_node > (1L << 31) - 1) return bad("too many elements or nodes");
+    if (!u.x || !u.y || !u.z || !u.nodelist || !u.lxim || !u.lxip || !u.letam || !u.letap || !u.lzetam ||
+        !u.lzetap)
+        return bad("NULL array");
+    const long NE = u.num_elem, NN = u.num_node;
+    const int *sets[4] = {u.symm_x, u.symm_y, u.symm_z, u.free_surf};
+    const long counts[4] = {u.num_symm_x, u.num_symm_y, u.num_symm_z, u.num_free_surf};
+    for (int t = 0; t < 4; ++t) {
+        if (counts[t] < 0 || (counts[t] > 0 && !sets[t])) return bad("bad node set");
+        for (long i = 0; i < counts[t]; ++i)
+            if (sets[t][i] < 0 || sets[t][i] >= NN) return bad("node set index out of range");
+    }
+    for (long i = 0; i < 8 * NE; ++i)
+        if (u.nodelist[i] < 0 || u.nodelist[i] >= NN) return bad("nodelist index out of range");
+    const int *nb[6] = {u.lxim, u.lxip, u.letam, u.letap, u.lzetam, u.lzetap};
+    for (int f = 0; f < 6; ++f)
+        for (long k = 0; k < NE; ++k)
+            if (nb[f][k] < 0 || nb[f][k] >= NE) return bad("face neighbour out of range");
+    {
+        std::vector<unsigned char> used(NN, 0);
+        for (long i = 0; i < 8 * NE; ++i) used[u.nodelist[i]] = 1;
+        for (long n = 0; n < NN; ++n)
+            if (!used[n]) return bad("node " + std::to_string(n) + " belongs to no element");
+    }
+
+    s = 0;
+    ne = NE;
+    nn = NN;
+    x.assign(u.x, u.x + NN);
+    y.assign(u.y, u.y + NN);
+    z.assign(u.z, u.z + NN);
+    nodelist.assign(u.nodelist, u.nodelist + 8 * NE);
+    lxim.assign(u.lxim, u.lxim + NE);
+    lxip.assign(u.lxip, u.lxip + NE);
+    letam.assign(u.letam, u.letam + NE);
+    letap.assign(u.letap, u.letap + NE);
+    lzetam.assign(u.lzetam, u.lzetam + NE);
+    lzetap.assign(u.lzetap, u.lzetap + NE);
+    derive();
+
+    // the symmetry node sets (lulesh.cu:810-838) as a per-node mask
+    node_bc.assign(NN, 0);
+    for (int t = 0; t < 3; ++t)
+        for (long i = 0; i < counts[t]; ++i) node_bc[sets[t][i]] |= (unsigned char)(1 << t);
+
+    elem_bc.assign(NE, 0);
+    std::vector<unsigned char> mark(NN, 0);
+    for (long n = 0; n < NN; ++n) mark[n] = node_bc[n] ? 1 : 0;
+    flag_faces(nodelist, mark, elem_bc);
+    origin = 0;
+    for (long k = 0; k < NE; ++k)
+        if (elem_bc[k] == (BC_XI_M_SYMM | BC_ETA_M_SYMM | BC_ZETA_M_SYMM)) {
+            origin = k;
+            break;
+        }
+    std::fill(mark.begin(), mark.end(), 0);
+    for (long i = 0; i < counts[3]; ++i) mark[sets[3][i]] = 1;
+    flag_faces(nodelist, mark, elem_bc);
+
+    e0 = 3.948746e+7;   // lulesh.cu:923
+    dt0 = 1.0e-7;       // lulesh.cu:999
+    return LULESH_OK;
+}
+
+// A whitespace-separated .lmesh file (the reader of lulesh.cu:733-850).
+int LmeshFile::read(const char *path, std::string *err)
+{
+    auto bad = [&](const std::string &m) {
+        if (err) *err = std::string("lmesh ") + (path ? path : "(null)") + ": " + m;
+        return LULESH_ERR_ARG;
+    };
+    if (!path) return bad("no path");
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return bad(std::string("cannot open: ") + std::strerror(errno));
+    std::string text;
+    char buf[1 << 16];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, got);
+    std::fclose(f);
+
+    const char *p = text.c_str();
+    bool ok = true;
+    auto next_long = [&]() -> long {
+        char *end;
+        const long v = std::strtol(p, &end, 10);
+        if (end == p) ok = false;
+        p = end;
+        return v;
+    };
+    auto next_double = [&]() -> double {
+        char *end;
+        const double v = std::strtod(p, &end);
+        if (end == p) ok = false;
+        p = end;
+        return v;
+    };
+    const long NE = next_long(), NN = next_long();
+    if (!ok || NE < 1 || NN < 1 || NE > (1L << 28) - 1 || NN > (1L << 31) - 1) return bad("bad header");
+    // each number takes at least two characters: refuse sizes the file cannot hold
+    if ((double)text.size() < 2.0 * (3.0 * NN + 14.0 * NE)) return bad("file shorter than its header says");
+    x.resize(NN);
+    y.resize(NN);
+    z.resize(NN);
+    for (long i = 0; i < NN && ok; ++i) {
+        x[i] = next_double();
+        y[i] = next_double();
+        z[i] = next_double();
+    }
+    nodelist.resize(8 * NE);
+    for (long i = 0; i < 8 * NE && ok; ++i) nodelist[i] = (int)next_long();
+    for (int f = 0; f < 6; ++f) nb[f].resize(NE);
+    for (long k = 0; k < NE && ok; ++k)
+        for (int f = 0; f < 6; ++f) nb[f][k] = (int)next_long();
+    for (int t = 0; t < 4 && ok; ++t) {
+        const long n = next_long();
+        if (!ok || n < 0 || n > NN) return bad("bad node-set size");
+        sets[t].resize(n);
+        for (long i = 0; i < n && ok; ++i) sets[t][i] = (int)next_long();
+    }
+    if (!ok) return bad("truncated or malformed");
+    view = lulesh_unstructured_mesh{};
+    view.num_elem = NE;
+    view.num_node = NN;
+    view.x = x.data();
+    view.y = y.data();
+    view.z = z.data();
+    view.nodelist = nodelist.data();
+    view.lxim = nb[0].data();
+    view.lxip = nb[1].data();
+    view.letam = nb[2].data();
+    view.letap = nb[3].data();
+    view.lzetam = nb[4].data();
+    view.lzetap = nb[5].data();
+    view.symm_x = sets[0].data();
+    view.symm_y = sets[1].data();
+    view.symm_z = sets[2].data();
+    view.free_surf = sets[3].data();
+    view.num_symm_x = (long)sets[0].size();
+    view.num_symm_y = (long)sets[1].size();
+    view.num_symm_z = (long)sets[2].size();
+    view.num_free_surf = (long)sets[3].size();
+    return LULESH_OK;
 }
 
 }  // namespace lulesh

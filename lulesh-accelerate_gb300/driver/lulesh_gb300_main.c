@@ -6,6 +6,10 @@
  * in the reference's format.  It uses only include/lulesh_gb300.h.
  *
  * Usage: lulesh_gb300_main S [--init v1|v2] [--split] [--cycles N] [--calls]
+ *        lulesh_gb300_main -u FILE.lmesh [--split] [--cycles N] [--calls]
+ *   -u       an unstructured mesh file, as the reference's GPU driver takes it
+ *            (reference/CUDA/lulesh-kepler-singlegpu/lulesh.cu:3321-3329);
+ *            the plane-0 symmetry test is then skipped, as there
  *   --calls  drive the loop from the host, one lulesh_time_increment +
  *            lulesh_lagrange_leapfrog call per cycle, as the reference's loop
  *            does (default: one lulesh_run call)
@@ -19,13 +23,15 @@
 
 int main(int argc, char **argv)
 {
-    if (argc < 2) {
-        fprintf(stderr, "usage: %s S [--init v1|v2] [--split] [--cycles N] [--calls]\n", argv[0]);
+    if (argc < 2 || (!strcmp(argv[1], "-u") && argc < 3)) {
+        fprintf(stderr, "usage: %s S [--init v1|v2] [--split] [--cycles N] [--calls]\n"
+                        "       %s -u FILE.lmesh [--split] [--cycles N] [--calls]\n", argv[0], argv[0]);
         return 2;
     }
-    const int s = atoi(argv[1]);
+    const char *lmesh = !strcmp(argv[1], "-u") ? argv[2] : NULL;
+    const int s = lmesh ? 0 : atoi(argv[1]);
     int init = LULESH_INIT_V2, precision = LULESH_PRECISION_FP64, cap = 0, calls = 0;
-    for (int i = 2; i < argc; ++i) {
+    for (int i = lmesh ? 3 : 2; i < argc; ++i) {
         if (!strcmp(argv[i], "--init") && i + 1 < argc) init = strcmp(argv[++i], "v1") ? LULESH_INIT_V2 : LULESH_INIT_V1;
         else if (!strcmp(argv[i], "--split")) precision = LULESH_PRECISION_SPLIT;
         else if (!strcmp(argv[i], "--cycles") && i + 1 < argc) cap = atoi(argv[++i]);
@@ -36,7 +42,8 @@ int main(int argc, char **argv)
         }
     }
     lulesh_ctx *ctx = NULL;
-    int rc = lulesh_create(s, init, precision, NULL, &ctx);
+    int rc = lmesh ? lulesh_create_lmesh(lmesh, precision, NULL, &ctx)
+                   : lulesh_create(s, init, precision, NULL, &ctx);
     if (rc) {
         fprintf(stderr, "lulesh_create: %d %s\n", rc, lulesh_last_error(NULL));
         return 1;
@@ -66,18 +73,23 @@ int main(int argc, char **argv)
     }
     const double elapsed = (double)(t1.tv_sec - t0.tv_sec) + 1e-6 * (double)(t1.tv_usec - t0.tv_usec);
     double e0 = 0.0, ma = 0.0, ta = 0.0, mr = 0.0;
+    long ne = 0;
     lulesh_origin_energy(ctx, &e0);
-    lulesh_symmetry(ctx, &ma, &ta, &mr);
+    lulesh_sizes(ctx, NULL, &ne, NULL);
+    if (!lmesh) lulesh_symmetry(ctx, &ma, &ta, &mr);
 
     printf("\n\nElapsed time = %12.6e\n\n", elapsed);
     printf("Run completed:  \n");
-    printf("   Problem size        =  %i \n", s);
+    if (lmesh) printf("   Problem size        =  %ld \n", ne);
+    else printf("   Problem size        =  %i \n", s);
     printf("   Iteration count     =  %i \n", cycles);
     printf("   Final Origin Energy = %12.6e \n", e0);
-    printf("   Testing Plane 0 of Energy Array:\n");
-    printf("        MaxAbsDiff   = %12.6e\n", ma);
-    printf("        TotalAbsDiff = %12.6e\n", ta);
-    printf("        MaxRelDiff   = %12.6e\n\n", mr);
+    if (!lmesh) {
+        printf("   Testing Plane 0 of Energy Array:\n");
+        printf("        MaxAbsDiff   = %12.6e\n", ma);
+        printf("        TotalAbsDiff = %12.6e\n", ta);
+        printf("        MaxRelDiff   = %12.6e\n\n", mr);
+    }
     printf("{\"cycles\": %d, \"origin_energy\": %.17e, \"max_rel_diff\": %.17e}\n", cycles, e0, mr);
     lulesh_destroy(ctx);
     return 0;

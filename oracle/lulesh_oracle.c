@@ -58,6 +58,8 @@ struct lo_domain {
     int *nodelist, *lxim, *lxip, *letam, *letap, *lzetam, *lzetap, *elem_bc;
     int *node_elem_start, *node_elem_count, *node_elem_corner_list;
     int *symm_x, *symm_y, *symm_z;
+    int nsymm_x, nsymm_y, nsymm_z;       /* (s+1)^2 each on the cube */
+    int origin;                          /* element holding the initial energy */
 };
 
 /* ------------------------------------------------------------------ */
@@ -452,10 +454,9 @@ int lo_lagrange_nodal(lo_domain *d)
         d->ydd[i] = d->fy[i] / d->nodal_mass[i];
         d->zdd[i] = d->fz[i] / d->nodal_mass[i];
     }
-    const int nbc = (d->s + 1) * (d->s + 1);
-    for (int i = 0; i < nbc; ++i) d->xdd[d->symm_x[i]] = 0.0;
-    for (int i = 0; i < nbc; ++i) d->ydd[d->symm_y[i]] = 0.0;
-    for (int i = 0; i < nbc; ++i) d->zdd[d->symm_z[i]] = 0.0;
+    for (int i = 0; i < d->nsymm_x; ++i) d->xdd[d->symm_x[i]] = 0.0;
+    for (int i = 0; i < d->nsymm_y; ++i) d->ydd[d->symm_y[i]] = 0.0;
+    for (int i = 0; i < d->nsymm_z; ++i) d->zdd[d->symm_z[i]] = 0.0;
 
 #pragma omp parallel for
     for (int i = 0; i < nn; ++i) {
@@ -873,7 +874,7 @@ int lo_run(lo_domain *d, int max_cycles, double *elapsed)
 /* LULESH-OMP.cc:3197-3223 */
 void lo_symmetry(lo_domain *d, double *max_abs, double *total_abs, double *max_rel)
 {
-    const int s = d->s;
+    const int s = d->s;                           /* 0 on an unstructured mesh: no test */
     double ma = 0.0, ta = 0.0, mr = 0.0;
     for (int j = 0; j < s; ++j)
         for (int k = j + 1; k < s; ++k) {
@@ -895,17 +896,12 @@ void lo_symmetry(lo_domain *d, double *max_abs, double *total_abs, double *max_r
 #define ALLOC_D(n) ((double *)calloc((size_t)(n), sizeof(double)))
 #define ALLOC_I(n) ((int *)calloc((size_t)(n), sizeof(int)))
 
-lo_domain *lo_create(int s, int init_mode)
+static lo_domain *alloc_domain(int ne, int nn, int nx, int ny, int nz)
 {
-    if (s < 1) return NULL;
     lo_domain *d = (lo_domain *)calloc(1, sizeof *d);
-    const int en = s + 1;
-    const int ne = s * s * s, nn = en * en * en;
-    d->s = s;
     d->nelem = ne;
     d->nnode = nn;
     lo_default_params(&d->prm);
-
     d->x = ALLOC_D(nn); d->y = ALLOC_D(nn); d->z = ALLOC_D(nn);
     d->xd = ALLOC_D(nn); d->yd = ALLOC_D(nn); d->zd = ALLOC_D(nn);
     d->xdd = ALLOC_D(nn); d->ydd = ALLOC_D(nn); d->zdd = ALLOC_D(nn);
@@ -928,7 +924,55 @@ lo_domain *lo_create(int s, int init_mode)
     d->elem_bc = ALLOC_I(ne);
     d->node_elem_start = ALLOC_I(nn); d->node_elem_count = ALLOC_I(nn);
     d->node_elem_corner_list = ALLOC_I(8L * ne);
-    d->symm_x = ALLOC_I(en * en); d->symm_y = ALLOC_I(en * en); d->symm_z = ALLOC_I(en * en);
+    d->nsymm_x = nx; d->nsymm_y = ny; d->nsymm_z = nz;
+    d->symm_x = ALLOC_I(nx > 0 ? nx : 1); d->symm_y = ALLOC_I(ny > 0 ? ny : 1);
+    d->symm_z = ALLOC_I(nz > 0 ? nz : 1);
+    return d;
+}
+
+/* Corner lists, reference volumes and masses of a filled-in nodelist. */
+static void mesh_derived(lo_domain *d)
+{
+    const int ne = d->nelem, nn = d->nnode;
+    /* node -> corner lists, AllocateNodeElemIndexes LULESH-OMP.cc:209-268:
+     * corners sorted by element, then by local corner number. */
+    for (int i = 0; i < 8 * ne; ++i) d->node_elem_count[d->nodelist[i]]++;
+    d->node_elem_start[0] = 0;
+    for (int i = 1; i < nn; ++i)
+        d->node_elem_start[i] = d->node_elem_start[i - 1] + d->node_elem_count[i - 1];
+    memset(d->node_elem_count, 0, sizeof(int) * (size_t)nn);
+    for (int i = 0; i < ne; ++i)
+        for (int j = 0; j < 8; ++j) {
+            const int m = d->nodelist[8 * i + j];
+            d->node_elem_corner_list[d->node_elem_start[m] + d->node_elem_count[m]] = 8 * i + j;
+            d->node_elem_count[m]++;
+        }
+
+    /* masses and reference volumes, LULESH-OMP.cc:3089-3109 */
+    for (int i = 0; i < ne; ++i) {
+        double x[8], y[8], z[8];
+        gather8(d->x, &d->nodelist[8 * i], x);
+        gather8(d->y, &d->nodelist[8 * i], y);
+        gather8(d->z, &d->nodelist[8 * i], z);
+        const double vol = elem_volume(x, y, z);
+        d->volo[i] = vol;
+        d->elem_mass[i] = vol;
+        for (int j = 0; j < 8; ++j) d->nodal_mass[d->nodelist[8 * i + j]] += vol / 8.0;
+    }
+    for (int i = 0; i < ne; ++i) d->v[i] = 1.0;
+    d->time = 0.0;
+    d->cycle = 0;
+    d->dtcourant = 1.0e+20;
+    d->dthydro = 1.0e+20;
+}
+
+lo_domain *lo_create(int s, int init_mode)
+{
+    if (s < 1) return NULL;
+    const int en = s + 1;
+    const int ne = s * s * s, nn = en * en * en;
+    lo_domain *d = alloc_domain(ne, nn, en * en, en * en, en * en);
+    d->s = s;
 
     /* coordinates, LULESH-OMP.cc:2996-3015 */
     int n = 0;
@@ -956,38 +1000,9 @@ lo_domain *lo_create(int s, int init_mode)
                 l[6] = n0 + en * en + en + 1;
                 l[7] = n0 + en * en + en;
             }
+    mesh_derived(d);
 
-    /* node -> corner lists, AllocateNodeElemIndexes LULESH-OMP.cc:209-268:
-     * corners sorted by element, then by local corner number. */
-    for (int i = 0; i < 8 * ne; ++i) d->node_elem_count[d->nodelist[i]]++;
-    d->node_elem_start[0] = 0;
-    for (int i = 1; i < nn; ++i)
-        d->node_elem_start[i] = d->node_elem_start[i - 1] + d->node_elem_count[i - 1];
-    memset(d->node_elem_count, 0, sizeof(int) * (size_t)nn);
-    for (int i = 0; i < ne; ++i)
-        for (int j = 0; j < 8; ++j) {
-            const int m = d->nodelist[8 * i + j];
-            d->node_elem_corner_list[d->node_elem_start[m] + d->node_elem_count[m]] = 8 * i + j;
-            d->node_elem_count[m]++;
-        }
-
-    /* masses and reference volumes, LULESH-OMP.cc:3089-3109 */
-    for (int i = 0; i < ne; ++i) {
-        double x[8], y[8], z[8];
-        gather8(d->x, &d->nodelist[8 * i], x);
-        gather8(d->y, &d->nodelist[8 * i], y);
-        gather8(d->z, &d->nodelist[8 * i], z);
-        const double vol = elem_volume(x, y, z);
-        d->volo[i] = vol;
-        d->elem_mass[i] = vol;
-        for (int j = 0; j < 8; ++j) d->nodal_mass[d->nodelist[8 * i + j]] += vol / 8.0;
-    }
-    for (int i = 0; i < ne; ++i) d->v[i] = 1.0;
-
-    d->time = 0.0;
-    d->cycle = 0;
-    d->dtcourant = 1.0e+20;
-    d->dthydro = 1.0e+20;
+    d->origin = 0;
     if (init_mode == LO_INIT_V2) {
         /* lulesh-2.0.3/lulesh-init.cc:171-182 */
         const double ebase = 3.948746e+7;
@@ -1032,6 +1047,79 @@ lo_domain *lo_create(int s, int init_mode)
     }
     return d;
 }
+
+/* Face flags from node sets, as the reference's unstructured reader sets
+ * them (reference/CUDA/lulesh-kepler-singlegpu/lulesh.cu:852-920): a face
+ * whose four corners all carry the mark gets the face's SYMM flag (the
+ * reader uses SYMM for its free-surface pass as well).  Corner bits 0-3 form
+ * the zeta- face, 4-7 zeta+, {0,1,4,5} eta-, {2,3,6,7} eta+, {0,3,4,7} xi-,
+ * {1,2,5,6} xi+. */
+static void flag_faces(lo_domain *d, const unsigned char *mark)
+{
+    for (int k = 0; k < d->nelem; ++k) {
+        int mask = 0;
+        for (int c = 0; c < 8; ++c) mask |= (mark[d->nodelist[8 * k + c]] ? 1 : 0) << c;
+        int *bc = &d->elem_bc[k];
+        if ((mask & 0x0f) == 0x0f) *bc |= BC_ZETA_M_SYMM;
+        if ((mask & 0xf0) == 0xf0) *bc |= BC_ZETA_P_SYMM;
+        if ((mask & 0x33) == 0x33) *bc |= BC_ETA_M_SYMM;
+        if ((mask & 0xcc) == 0xcc) *bc |= BC_ETA_P_SYMM;
+        if ((mask & 0x99) == 0x99) *bc |= BC_XI_M_SYMM;
+        if ((mask & 0x66) == 0x66) *bc |= BC_XI_P_SYMM;
+    }
+}
+
+/* An unstructured mesh, set up as the reference's unstructured reader does
+ * (lulesh.cu:733-923): LULESH 1.0 initial energy 3.948746e7 in the origin
+ * element (the first flagged SYMM on its xi-, eta- and zeta- faces by the
+ * symmetry pass; element 0 if none is) and dt0 = 1e-7. */
+lo_domain *lo_create_mesh(const lo_mesh *m)
+{
+    if (!m || m->nelem < 1 || m->nnode < 1) return NULL;
+    const int ne = m->nelem, nn = m->nnode;
+    for (long i = 0; i < 8L * ne; ++i)
+        if (m->nodelist[i] < 0 || m->nodelist[i] >= nn) return NULL;
+    const int *nb[6] = {m->lxim, m->lxip, m->letam, m->letap, m->lzetam, m->lzetap};
+    for (int f = 0; f < 6; ++f)
+        for (int k = 0; k < ne; ++k)
+            if (nb[f][k] < 0 || nb[f][k] >= ne) return NULL;
+    const int *sets[4] = {m->symm_x, m->symm_y, m->symm_z, m->free_surf};
+    const int counts[4] = {m->nsymm_x, m->nsymm_y, m->nsymm_z, m->nfree};
+    for (int t = 0; t < 4; ++t)
+        for (int i = 0; i < counts[t]; ++i)
+            if (sets[t][i] < 0 || sets[t][i] >= nn) return NULL;
+
+    lo_domain *d = alloc_domain(ne, nn, m->nsymm_x, m->nsymm_y, m->nsymm_z);
+    d->s = 0;
+    memcpy(d->x, m->x, sizeof(double) * (size_t)nn);
+    memcpy(d->y, m->y, sizeof(double) * (size_t)nn);
+    memcpy(d->z, m->z, sizeof(double) * (size_t)nn);
+    memcpy(d->nodelist, m->nodelist, sizeof(int) * 8 * (size_t)ne);
+    int *dst[6] = {d->lxim, d->lxip, d->letam, d->letap, d->lzetam, d->lzetap};
+    for (int f = 0; f < 6; ++f) memcpy(dst[f], nb[f], sizeof(int) * (size_t)ne);
+    memcpy(d->symm_x, m->symm_x, sizeof(int) * (size_t)m->nsymm_x);
+    memcpy(d->symm_y, m->symm_y, sizeof(int) * (size_t)m->nsymm_y);
+    memcpy(d->symm_z, m->symm_z, sizeof(int) * (size_t)m->nsymm_z);
+    mesh_derived(d);
+
+    unsigned char *mark = (unsigned char *)calloc((size_t)nn, 1);
+    for (int t = 0; t < 3; ++t)
+        for (int i = 0; i < counts[t]; ++i) mark[sets[t][i]] = 1;
+    flag_faces(d, mark);
+    d->origin = 0;
+    for (int k = 0; k < ne; ++k)
+        if (d->elem_bc[k] == (BC_XI_M_SYMM | BC_ETA_M_SYMM | BC_ZETA_M_SYMM)) { d->origin = k; break; }
+    memset(mark, 0, (size_t)nn);
+    for (int i = 0; i < m->nfree; ++i) mark[m->free_surf[i]] = 1;
+    flag_faces(d, mark);
+    free(mark);
+
+    d->e[d->origin] = 3.948746e+7;
+    d->deltatime = 1.0e-7;
+    return d;
+}
+
+int lo_origin(lo_domain *d) { return d->origin; }
 
 void lo_destroy(lo_domain *d)
 {
@@ -1087,7 +1175,6 @@ double *lo_field(lo_domain *d, const char *name, long *len)
 
 int *lo_ifield(lo_domain *d, const char *name, long *len)
 {
-    const long en2 = (long)(d->s + 1) * (d->s + 1);
     const struct { const char *n; int *p; long l; } t[] = {
         {"nodelist", d->nodelist, 8L * d->nelem},
         {"lxim", d->lxim, d->nelem}, {"lxip", d->lxip, d->nelem},
@@ -1097,7 +1184,8 @@ int *lo_ifield(lo_domain *d, const char *name, long *len)
         {"nodeElemStart", d->node_elem_start, d->nnode},
         {"nodeElemCount", d->node_elem_count, d->nnode},
         {"nodeElemCornerList", d->node_elem_corner_list, 8L * d->nelem},
-        {"symmX", d->symm_x, en2}, {"symmY", d->symm_y, en2}, {"symmZ", d->symm_z, en2},
+        {"symmX", d->symm_x, d->nsymm_x}, {"symmY", d->symm_y, d->nsymm_y},
+        {"symmZ", d->symm_z, d->nsymm_z},
     };
     for (size_t i = 0; i < sizeof t / sizeof t[0]; ++i)
         if (!strcmp(name, t[i].n)) { if (len) *len = t[i].l; return t[i].p; }

@@ -43,8 +43,25 @@ typedef struct lo_params {
 
 typedef struct lo_domain lo_domain;
 
+/* An unstructured hexahedral mesh (the reference's .lmesh contents): node
+ * coordinates, 8 nodes per element in the reference's corner order, the six
+ * face neighbours of each element (the element itself on a boundary), the
+ * symmetry-plane node sets and the free-surface node set. */
+typedef struct lo_mesh {
+    int nelem, nnode;
+    const double *x, *y, *z;
+    const int *nodelist;
+    const int *lxim, *lxip, *letam, *letap, *lzetam, *lzetap;
+    const int *symm_x, *symm_y, *symm_z, *free_surf;
+    int nsymm_x, nsymm_y, nsymm_z, nfree;
+} lo_mesh;
+
 void        lo_default_params(lo_params *p);
 lo_domain  *lo_create(int s, int init_mode);
+/* NULL for an empty mesh or an index out of range. */
+lo_domain  *lo_create_mesh(const lo_mesh *m);
+/* Element holding the initial energy (0 on the cube). */
+int         lo_origin(lo_domain *d);
 void        lo_destroy(lo_domain *d);
 lo_params  *lo_params_of(lo_domain *d);
 

@@ -31,6 +31,50 @@ INT_FIELDS = ("nodelist", "lxim", "lxip", "letam", "letap", "lzetam", "lzetap", 
               "nodeElemStart", "nodeElemCount", "nodeElemCornerList", "symmX", "symmY", "symmZ")
 
 
+class Mesh(C.Structure):
+    """lo_mesh: an unstructured hexahedral mesh."""
+    _fields_ = [("nelem", C.c_int), ("nnode", C.c_int),
+                ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)), ("z", C.POINTER(C.c_double)),
+                ("nodelist", C.POINTER(C.c_int))] + \
+               [(n, C.POINTER(C.c_int)) for n in ("lxim", "lxip", "letam", "letap", "lzetam", "lzetap",
+                                                 "symm_x", "symm_y", "symm_z", "free_surf")] + \
+               [(n, C.c_int) for n in ("nsymm_x", "nsymm_y", "nsymm_z", "nfree")]
+
+
+def read_lmesh(path) -> dict:
+    """The contents of a .lmesh file as numpy arrays.
+
+    Layout (the reference's unstructured reader,
+    reference/CUDA/lulesh-kepler-singlegpu/lulesh.cu:733-850): numElem numNode;
+    numNode coordinate triples; 8 node indices per element; 6 face
+    neighbours per element (xi-, xi+, eta-, eta+, zeta-, zeta+); then the
+    symmetry X, Y, Z and free-surface node sets, each a count and indices.
+    """
+    import gzip
+    raw = Path(path).read_bytes()
+    if raw[:2] == b"\x1f\x8b":
+        raw = gzip.decompress(raw)
+    tok = raw.split()
+    ne, nn = int(tok[0]), int(tok[1])
+    off = 2
+    xyz = np.array(tok[off:off + 3 * nn], dtype=np.float64).reshape(nn, 3)
+    off += 3 * nn
+    nodelist = np.array(tok[off:off + 8 * ne], dtype=np.int32)
+    off += 8 * ne
+    nb = np.array(tok[off:off + 6 * ne], dtype=np.int32).reshape(ne, 6)
+    off += 6 * ne
+    sets = []
+    for _ in range(4):
+        n = int(tok[off])
+        sets.append(np.array(tok[off + 1:off + 1 + n], dtype=np.int32))
+        off += 1 + n
+    m = {"nelem": ne, "nnode": nn, "x": xyz[:, 0].copy(), "y": xyz[:, 1].copy(), "z": xyz[:, 2].copy(),
+         "nodelist": nodelist, "symm_x": sets[0], "symm_y": sets[1], "symm_z": sets[2], "free_surf": sets[3]}
+    for i, n in enumerate(("lxim", "lxip", "letam", "letap", "lzetam", "lzetap")):
+        m[n] = np.ascontiguousarray(nb[:, i])
+    return m
+
+
 class Params(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "e_cut", "p_cut", "q_cut", "v_cut", "u_cut",
@@ -56,6 +100,10 @@ def lib():
         L = C.CDLL(str(LIB))
         L.lo_create.restype = C.c_void_p
         L.lo_create.argtypes = [C.c_int, C.c_int]
+        L.lo_create_mesh.restype = C.c_void_p
+        L.lo_create_mesh.argtypes = [C.POINTER(Mesh)]
+        L.lo_origin.restype = C.c_int
+        L.lo_origin.argtypes = [C.c_void_p]
         L.lo_destroy.argtypes = [C.c_void_p]
         L.lo_params_of.restype = C.POINTER(Params)
         L.lo_params_of.argtypes = [C.c_void_p]
@@ -84,11 +132,34 @@ def lib():
 class Oracle:
     """One Sedov problem in the oracle; fields are live numpy views."""
 
-    def __init__(self, s: int, init: int = INIT_V2):
+    def __init__(self, s: int, init: int = INIT_V2, *, mesh: dict | None = None):
+        if mesh is not None:
+            self._keep = {k: np.ascontiguousarray(v, dtype=np.float64 if k in "xyz" else np.int32)
+                          for k, v in mesh.items() if isinstance(v, np.ndarray)}
+            m = Mesh(nelem=mesh["nelem"], nnode=mesh["nnode"])
+            for k, v in self._keep.items():
+                ct = C.c_double if v.dtype == np.float64 else C.c_int
+                setattr(m, k, v.ctypes.data_as(C.POINTER(ct)))
+            m.nsymm_x, m.nsymm_y, m.nsymm_z = (len(mesh[k]) for k in ("symm_x", "symm_y", "symm_z"))
+            m.nfree = len(mesh["free_surf"])
+            self._h = lib().lo_create_mesh(C.byref(m))
+            if not self._h:
+                raise ValueError("bad mesh")
+            self.s = 0
+            return
         self._h = lib().lo_create(s, init)
         if not self._h:
             raise ValueError(f"bad size {s}")
         self.s = s
+
+    @classmethod
+    def from_mesh(cls, mesh: dict) -> "Oracle":
+        """An unstructured problem (read_lmesh's dictionary)."""
+        return cls(0, mesh=mesh)
+
+    @property
+    def origin(self) -> int:
+        return lib().lo_origin(self._h)
 
     def close(self):
         if self._h:

@@ -13,9 +13,14 @@
  *   - the mesh set-up of the reference's main() (:2960-3171), restated, with
  *     a choice of LULESH 1.0 (e0 = 3.948746e7, dt0 = 1e-7) or LULESH 2.0
  *     initial energy and time step (lulesh-2.0.3/lulesh-init.cc:171-182);
+ *   - an unstructured mesh read from a .lmesh file (-u FILE), set up as the
+ *     reference's unstructured reader does
+ *     (reference/CUDA/lulesh-kepler-singlegpu/lulesh.cu:733-923, restated);
  *   - a cycle cap, full-precision JSON output and binary state dumps.
  *
  * Usage: lulesh_ref S [--init v1|v2] [--cycles N] [--warmup W] [--dump FILE]
+ *                     [--phase-dump FILE CYCLE]
+ *        lulesh_ref -u FILE.lmesh [--cycles N] [--warmup W] [--dump FILE]
  *                     [--phase-dump FILE CYCLE]
  * (--warmup W: the first W cycles run before the timer starts; they count
  * towards --cycles.)
@@ -220,6 +225,154 @@ void setup(Index_t edgeElems, bool v2)
     }
 }
 
+/* Parameters of LULESH-OMP.cc:3051-3087 (both mesh kinds). */
+void set_params()
+{
+    domain.dtfixed() = Real_t(-1.0e-7);
+    domain.deltatime() = Real_t(1.0e-7);
+    domain.deltatimemultlb() = Real_t(1.1);
+    domain.deltatimemultub() = Real_t(1.2);
+    domain.stoptime() = Real_t(1.0e-2);
+    domain.dtcourant() = Real_t(1.0e+20);
+    domain.dthydro() = Real_t(1.0e+20);
+    domain.dtmax() = Real_t(1.0e-2);
+    domain.time() = Real_t(0.);
+    domain.cycle() = 0;
+    domain.e_cut() = Real_t(1.0e-7);
+    domain.p_cut() = Real_t(1.0e-7);
+    domain.q_cut() = Real_t(1.0e-7);
+    domain.u_cut() = Real_t(1.0e-7);
+    domain.v_cut() = Real_t(1.0e-10);
+    domain.hgcoef() = Real_t(3.0);
+    domain.ss4o3() = Real_t(4.0) / Real_t(3.0);
+    domain.qstop() = Real_t(1.0e+12);
+    domain.monoq_max_slope() = Real_t(1.0);
+    domain.monoq_limiter_mult() = Real_t(2.0);
+    domain.qlc_monoq() = Real_t(0.5);
+    domain.qqc_monoq() = Real_t(2.0) / Real_t(3.0);
+    domain.qqc() = Real_t(2.0);
+    domain.pmin() = Real_t(0.);
+    domain.emin() = Real_t(-1.0e+15);
+    domain.dvovmax() = Real_t(0.1);
+    domain.eosvmax() = Real_t(1.0e+9);
+    domain.eosvmin() = Real_t(1.0e-9);
+    domain.refdens() = Real_t(1.0);
+}
+
+/* Unstructured set-up from a .lmesh file.  The file holds, as whitespace-
+ * separated numbers: numElem numNode; numNode coordinate triples; 8 node
+ * indices per element; 6 face neighbours per element (xi-, xi+, eta-, eta+,
+ * zeta-, zeta+); then four node sets, each a count and its indices:
+ * symmetry X, Y, Z and the free surface.
+ *
+ * The reference's step applies its symmetry sets over (sizeX+1)^2 entries
+ * (ApplyAccelerationBoundaryConditionsForNodes, LULESH-OMP.cc:1626-1645), so
+ * sizeX is chosen to make (sizeX+1)^2 cover the largest set and each set is
+ * padded by repeating its last node (zeroing the same acceleration twice is
+ * harmless).  Element face flags follow the reference's unstructured reader:
+ * a face whose four corners all lie in the union of the symmetry sets, and
+ * then a face whose four corners all lie in the free-surface set, is marked
+ * SYMM; the origin element is the first one flagged SYMM on its xi-, eta- and
+ * zeta- faces by the first pass. */
+Index_t setup_unstructured(const char *path)
+{
+    FILE *fp = fopen(path, "r");
+    if (!fp) { fprintf(stderr, "could not open %s\n", path); exit(2); }
+    auto rd_i = [&](void) { int v; if (fscanf(fp, "%d", &v) != 1) { fprintf(stderr, "bad lmesh %s\n", path); exit(2); } return v; };
+    auto rd_d = [&](void) { double v; if (fscanf(fp, "%lf", &v) != 1) { fprintf(stderr, "bad lmesh %s\n", path); exit(2); } return v; };
+    const Index_t ne = rd_i(), nn = rd_i();
+    domain.numElem() = ne;
+    domain.numNode() = nn;
+    domain.AllocateElemPersistent(ne);
+    domain.AllocateElemTemporary(ne);
+    domain.AllocateNodalPersistent(nn);
+    for (Index_t i = 0; i < nn; ++i) {
+        domain.x(i) = Real_t(rd_d());
+        domain.y(i) = Real_t(rd_d());
+        domain.z(i) = Real_t(rd_d());
+    }
+    for (Index_t k = 0; k < ne; ++k) {
+        Index_t *l = domain.nodelist(k);
+        for (int c = 0; c < 8; ++c) l[c] = rd_i();
+    }
+    for (Index_t k = 0; k < ne; ++k) {
+        domain.lxim(k) = rd_i();  domain.lxip(k) = rd_i();
+        domain.letam(k) = rd_i(); domain.letap(k) = rd_i();
+        domain.lzetam(k) = rd_i(); domain.lzetap(k) = rd_i();
+    }
+    std::vector<Index_t> sets[4];
+    for (int t = 0; t < 4; ++t) {
+        const int n = rd_i();
+        sets[t].resize(n);
+        for (int i = 0; i < n; ++i) sets[t][i] = rd_i();
+    }
+    fclose(fp);
+
+    size_t most = 1;
+    for (int t = 0; t < 3; ++t) {
+        if (sets[t].empty()) { fprintf(stderr, "empty symmetry set in %s\n", path); exit(2); }
+        most = std::max(most, sets[t].size());
+    }
+    Index_t side = 1;
+    while (size_t(side) * size_t(side) < most) ++side;
+    domain.sizeX() = domain.sizeY() = domain.sizeZ() = side - 1;
+    domain.AllocateNodesets(size_t(side) * size_t(side));
+    for (size_t i = 0; i < size_t(side) * size_t(side); ++i) {
+        domain.symmX(i) = sets[0][std::min(i, sets[0].size() - 1)];
+        domain.symmY(i) = sets[1][std::min(i, sets[1].size() - 1)];
+        domain.symmZ(i) = sets[2][std::min(i, sets[2].size() - 1)];
+    }
+
+    domain.AllocateNodeElemIndexes();
+    for (Index_t i = 0; i < ne; ++i) domain.matElemlist(i) = i;
+    set_params();
+
+    for (Index_t i = 0; i < ne; ++i) {
+        Real_t xl[8], yl[8], zl[8];
+        Index_t *nl = domain.nodelist(i);
+        for (int k = 0; k < 8; ++k) {
+            xl[k] = domain.x(nl[k]);
+            yl[k] = domain.y(nl[k]);
+            zl[k] = domain.z(nl[k]);
+        }
+        const Real_t volume = CalcElemVolume(xl, yl, zl);
+        domain.volo(i) = volume;
+        domain.elemMass(i) = volume;
+        for (int k = 0; k < 8; ++k) domain.nodalMass(nl[k]) += volume / Real_t(8.0);
+    }
+
+    /* face flags from the corner masks: bits 0-3 are the zeta- face,
+     * 4-7 zeta+, {0,1,4,5} eta-, {2,3,6,7} eta+, {0,3,4,7} xi-, {1,2,5,6} xi+ */
+    auto flag_faces = [&](const std::vector<char> &on) {
+        for (Index_t k = 0; k < ne; ++k) {
+            const Index_t *l = domain.nodelist(k);
+            int mask = 0;
+            for (int c = 0; c < 8; ++c) mask |= (on[l[c]] ? 1 : 0) << c;
+            Int_t &bc = domain.elemBC(k);
+            if ((mask & 0x0f) == 0x0f) bc |= ZETA_M_SYMM;
+            if ((mask & 0xf0) == 0xf0) bc |= ZETA_P_SYMM;
+            if ((mask & 0x33) == 0x33) bc |= ETA_M_SYMM;
+            if ((mask & 0xcc) == 0xcc) bc |= ETA_P_SYMM;
+            if ((mask & 0x99) == 0x99) bc |= XI_M_SYMM;
+            if ((mask & 0x66) == 0x66) bc |= XI_P_SYMM;
+        }
+    };
+    for (Index_t k = 0; k < ne; ++k) domain.elemBC(k) = 0;
+    std::vector<char> on(nn, 0);
+    for (int t = 0; t < 3; ++t)
+        for (Index_t n : sets[t]) on[n] = 1;
+    flag_faces(on);
+    Index_t origin = 0;
+    for (Index_t k = 0; k < ne; ++k)
+        if (domain.elemBC(k) == (XI_M_SYMM | ETA_M_SYMM | ZETA_M_SYMM)) { origin = k; break; }
+    std::fill(on.begin(), on.end(), 0);
+    for (Index_t n : sets[3]) on[n] = 1;
+    flag_faces(on);
+
+    domain.e(origin) = Real_t(3.948746e+7);
+    return origin;
+}
+
 }  // namespace
 
 int main(int argc, char *argv[])
@@ -229,11 +382,13 @@ int main(int argc, char *argv[])
                         "[--phase-dump FILE CYCLE]\n", argv[0]);
         return 2;
     }
-    const int s = atoi(argv[1]);
+    const bool unstructured = !strcmp(argv[1], "-u");
+    if (unstructured && argc < 3) return 2;
+    const int s = unstructured ? 0 : atoi(argv[1]);
     bool v2 = true;
     int max_cycles = 0, phase_cycle = -1, warmup = 0;
     const char *dump_path = NULL, *phase_path = NULL;
-    for (int i = 2; i < argc; ++i) {
+    for (int i = unstructured ? 3 : 2; i < argc; ++i) {
         if (!strcmp(argv[i], "--init") && i + 1 < argc) v2 = strcmp(argv[++i], "v1") != 0;
         else if (!strcmp(argv[i], "--cycles") && i + 1 < argc) max_cycles = atoi(argv[++i]);
         else if (!strcmp(argv[i], "--warmup") && i + 1 < argc) warmup = atoi(argv[++i]);
@@ -246,8 +401,14 @@ int main(int argc, char *argv[])
             return 2;
         }
     }
-    if (s < 1) return 2;
-    setup(s, v2);
+    Index_t origin = 0;
+    if (unstructured) {
+        origin = setup_unstructured(argv[2]);
+        v2 = false;
+    } else {
+        if (s < 1) return 2;
+        setup(s, v2);
+    }
 
     FILE *pf = phase_path ? fopen(phase_path, "wb") : NULL;
     timeval start, end;
@@ -291,11 +452,11 @@ int main(int argc, char *argv[])
     }
     const int timed = n > warmup ? n - warmup : n;
     const double zc = double(domain.numElem()) * double(timed);
-    printf("{\"s\": %d, \"init\": \"%s\", \"cycles\": %d, \"origin_energy\": %.17e, "
+    printf("{\"s\": %d, \"init\": \"%s\", \"origin_elem\": %d, \"num_elem\": %d, \"cycles\": %d, \"origin_energy\": %.17e, "
            "\"time\": %.17e, \"deltatime\": %.17e, \"dtcourant\": %.17e, \"dthydro\": %.17e, "
            "\"max_abs_diff\": %.17e, \"total_abs_diff\": %.17e, \"max_rel_diff\": %.17e, "
            "\"elapsed_s\": %.6f, \"timed_cycles\": %d, \"threads\": %d, \"mzone_cycles_per_s\": %.6f}\n",
-           s, v2 ? "v2" : "v1", domain.cycle(), double(domain.e(0)), double(domain.time()),
+           s, v2 ? "v2" : "v1", int(origin), int(domain.numElem()), domain.cycle(), double(domain.e(origin)), double(domain.time()),
            double(domain.deltatime()), double(domain.dtcourant()), double(domain.dthydro()),
            double(MaxAbsDiff), double(TotalAbsDiff), double(MaxRelDiff), elapsed, timed,
            omp_get_max_threads(), elapsed > 0 ? zc / elapsed * 1e-6 : 0.0);

@@ -47,8 +47,8 @@ def find_run(answers, s, init, cap=0):
     raise KeyError((s, init, cap))
 
 
-def load_phases(s, cyc):
-    z = np.load(GOLDEN / f"phases_s{s}_c{cyc}.npz")
+def load_phases(s, cyc, mesh=None):
+    z = np.load(GOLDEN / (f"phases_{mesh}_c{cyc}.npz" if mesh else f"phases_s{s}_c{cyc}.npz"))
     stages = {}
     for key in z.files:
         st, name = key.split("/")
