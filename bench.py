@@ -18,6 +18,10 @@ Legs of the default run (one JSON line on rank 0):
                with its status/scalar read-back, download of the final state
   cpu_baseline the reference CPU implementation on this host's cores, a
                bounded sample of the same workload
+  split        the same workload in split precision
+  batched      the seeded ensembles (64 FP64 instances; 528 split instances)
+  regions      LULESH 2.0 material regions with EOS cost (-r 11 -b 1 -c 1) on
+               the same mesh, beside the unmodified LULESH 2.0 program
 
 ``--impl reference`` times only the reference CPU implementation (the
 reference has no GPU path for this workload that runs on sm_103a).
@@ -29,12 +33,15 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
 import tempfile
 import time
 from pathlib import Path
+
+import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
@@ -154,6 +161,41 @@ def cpu_run(s: int, warmup: int, cycles: int, threads: int) -> dict:
             "elapsed_s": r["elapsed_s"], "cycles": r["timed_cycles"],
             "sample": f"s={s} LULESH 2.0 initial conditions, {r['timed_cycles']} cycles after "
                       f"{warmup} warm-up cycles, {r['threads']} OpenMP threads"}
+
+
+def lulesh2_run(s: int, iters: int, regions: int, balance: int, cost: int, threads: int) -> dict | None:
+    """The unmodified LULESH 2.0 program (regions and EOS cost), built from the
+    reference's sources by build(); None where it could not be built."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    exe = oracle.HERE / "_ref" / "lulesh2"
+    if not exe.exists():
+        return None
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    out = subprocess.run([str(exe), "-s", str(s), "-i", str(iters), "-r", str(regions), "-b", str(balance),
+                          "-c", str(cost)], capture_output=True, text=True, env=env, check=True).stdout
+    grind_us = float(re.search(r"Grind time \(us/z/c\)\s*=\s*(\S+)", out).group(1))
+    return {"value": 1.0 / grind_us, "unit": UNIT, "cores": threads, "kind": "reference",
+            "sample": f"lulesh-2.0.3 -s {s} -i {iters} -r {regions} -b {balance} -c {cost}, "
+                      f"{threads} OpenMP threads (its grind time)"}
+
+
+def regions_leg(pkg, args, timed, plain_value) -> dict:
+    """LULESH 2.0 regions and EOS cost (-r 11 -b 1 -c 1, its defaults) on the
+    headline mesh: same results, more EOS work in the costly regions."""
+    nr, bal, cost = 11, 1, 1
+    g = pkg.Lulesh(args.size, pkg.INIT_V2, pkg.FP64)
+    g.set_regions(nr, bal, cost)
+    reps = np.array([1 if r - 1 < nr // 2 else (1 + cost if r - 1 < nr - (nr + 15) // 20 else 10 * (1 + cost))
+                     for r in range(1, nr + 1)])
+    mean_rep = float(reps[g.regions() - 1].mean())
+    ms, launches = timed(g, args.region_steps)
+    value = g.num_elem * args.region_steps / (ms * 1e-3) * 1e-6
+    g.close()
+    return {"value": value, "unit": UNIT, "ms_per_step": ms / args.region_steps, "steps": args.region_steps,
+            "regions": nr, "balance": bal, "cost": cost, "mean_eos_evaluations": mean_rep,
+            "vs_plain_fp64": value / plain_value, "gpu_launches": launches}
 
 
 def batch_legs(pkg, torch, args, barrier, max_over_ranks) -> dict:
@@ -307,6 +349,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-split", action="store_true", help="skip the split-precision leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble legs")
+    ap.add_argument("--no-regions", action="store_true", help="skip the LULESH 2.0 regions leg")
+    ap.add_argument("--region-steps", type=int, default=100, help="timed cycles of the regions leg")
     ap.add_argument("--solo-seconds", type=float, default=8.0,
                     help="budget of the one-at-a-time sample of each batched leg")
     ap.add_argument("--launch", default="graph", choices=["graph", "direct"],
@@ -456,6 +500,12 @@ def main():
     if args.precision == "fp64" and not args.no_batch:
         batched = batch_legs(pkg, torch, args, barrier, max_over_ranks)
 
+    regions = None
+    if args.precision == "fp64" and not args.no_regions:
+        regions = regions_leg(pkg, args, timed, value / world)
+        if rank == 0 and not args.no_cpu:
+            regions["cpu_baseline"] = lulesh2_run(args.size, 3, 11, 1, 1, os.cpu_count() or 1)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_run(args.size, 2, args.cpu_cycles, os.cpu_count() or 1)
@@ -471,7 +521,7 @@ def main():
                 "bytes_per_zone_cycle": cycle_bytes,
                 "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks.summary(), "results": ref_metrics, "split": split,
-                "batched": batched}
+                "batched": batched, "regions": regions}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

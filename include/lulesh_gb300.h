@@ -193,6 +193,27 @@ int lulesh_keep_forces(lulesh_ctx *ctx, int keep);
 int lulesh_set_params(lulesh_ctx *ctx, const lulesh_params *params);
 int lulesh_get_params(lulesh_ctx *ctx, lulesh_params *params);
 
+/* ---- LULESH 2.0 regions ------------------------------------------------
+ * lulesh_set_regions splits the elements into num_regions material regions
+ * as LULESH 2.0 does on one rank (Domain::CreateRegionIndexSets,
+ * lulesh-2.0.3/lulesh-init.cc:377-486, its -r/-b/-c options
+ * lulesh-util.cc:95-136): runs of consecutive elements, each run's region
+ * drawn with weight (r+1)^balance from the C library generator seeded with
+ * 0, run lengths from the reference's bin table.  Every region is the same
+ * material, so results do not change; what changes is the work: the EOS of
+ * an element in region r (0-based) is evaluated 1, 1+cost or 10*(1+cost)
+ * times (ApplyMaterialPropertiesForElems, lulesh.cc:2410-2424).
+ * num_regions = 0 removes the regions (one EOS evaluation per element, the
+ * LULESH 1.0 / LULESH-OMP.cc behaviour and the default).  LULESH_ERR_ARG for
+ * negative arguments, cost > 100 or weights that overflow an int.
+ * lulesh_get_regions writes each element's region number (1..num_regions;
+ * all 1 without regions) into reg_num_list [num_elem] (regNumList). */
+int lulesh_set_regions(lulesh_ctx *ctx, int num_regions, int balance, int cost);
+int lulesh_get_regions(lulesh_ctx *ctx, int *reg_num_list);
+/* The same assignment on the host, without a context: region numbers of
+ * num_elem elements into reg_num_list [num_elem]. */
+int lulesh_region_numbers(long num_elem, int num_regions, int balance, int *reg_num_list);
+
 /* ---- the step API ---------------------------------------------------- */
 int lulesh_time_increment(lulesh_ctx *ctx);        /* TimeIncrement      LULESH-OMP.cc:557-604   */
 int lulesh_lagrange_nodal(lulesh_ctx *ctx);        /* LagrangeNodal      LULESH-OMP.cc:1685-1704 */

@@ -116,6 +116,9 @@ _SIGNATURES = {
                                              C.POINTER(C.c_void_p)]),
     "lulesh_create_lmesh": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(Parameters), C.POINTER(C.c_void_p)]),
     "lulesh_origin_element": (C.c_int, [C.c_void_p, C.POINTER(C.c_long)]),
+    "lulesh_set_regions": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "lulesh_get_regions": (C.c_int, [C.c_void_p, _ip]),
+    "lulesh_region_numbers": (C.c_int, [C.c_long, C.c_int, C.c_int, _ip]),
     "lulesh_destroy": (None, [C.c_void_p]),
     "lulesh_last_error": (C.c_char_p, [C.c_void_p]),
     "lulesh_upload_domain": (C.c_int, [C.c_void_p] + [_dp] * 11 + [C.c_double, C.c_double]),
@@ -203,6 +206,13 @@ def default_parameters() -> Parameters:
     p = Parameters()
     load_library().lulesh_default_params(C.byref(p))
     return p
+
+
+def region_numbers(num_elem: int, num_regions: int, balance: int = 1) -> np.ndarray:
+    """LULESH 2.0's element-to-region assignment, computed on the host."""
+    out = np.empty(num_elem, dtype=np.int32)
+    _check(load_library().lulesh_region_numbers(num_elem, num_regions, balance, _ptr(out, C.c_int)))
+    return out
 
 
 def mesh_sizes(s: int) -> tuple[int, int]:
@@ -313,6 +323,18 @@ class Lulesh:
             os.fsencode(str(path)), precision, C.byref(params) if params is not None else None, C.byref(h))
         _check(rc)
         return cls(0, _handle=h)
+
+    def set_regions(self, num_regions: int = 11, balance: int = 1, cost: int = 1) -> None:
+        """LULESH 2.0 material regions (its -r/-b/-c options; defaults are its
+        defaults).  Results do not change; the EOS of costly regions runs
+        1+cost or 10*(1+cost) times.  ``num_regions=0`` removes them."""
+        _check(load_library().lulesh_set_regions(self._h, num_regions, balance, cost), self._h)
+
+    def regions(self) -> np.ndarray:
+        """Region number (1-based) of every element."""
+        out = np.empty(self.num_elem, dtype=np.int32)
+        _check(load_library().lulesh_get_regions(self._h, _ptr(out, C.c_int)), self._h)
+        return out
 
     @property
     def origin(self) -> int:

@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -31,6 +33,8 @@ struct lulesh_ctx {
     int status = LULESH_OK;          // sticky step error
     long long launches = 0;
     long origin = 0;                 // element holding the initial energy
+    std::vector<int> regions;        // LULESH 2.0 region number per element (empty: none)
+    int *d_mat_order = nullptr, *d_reps = nullptr;
     std::string err;
 };
 
@@ -493,6 +497,52 @@ int lulesh_keep_forces(lulesh_ctx *ctx, int keep)
     if (ctx->run_exec) { cudaGraphExecDestroy(ctx->run_exec); ctx->run_exec = nullptr; }
     if (ctx->chunk_exec) { cudaGraphExecDestroy(ctx->chunk_exec); ctx->chunk_exec = nullptr; }
     ctx->run_mode = 0;
+    return LULESH_OK;
+}
+
+int lulesh_set_regions(lulesh_ctx *ctx, int num_regions, int balance, int cost)
+{
+    if (!ctx) return LULESH_ERR_ARG;
+    if (num_regions < 0 || balance < 0 || cost < 0 || cost > 100)
+        return fail(ctx, LULESH_ERR_ARG, "lulesh_set_regions: need num_regions >= 0, balance >= 0, 0 <= cost <= 100");
+    double weights = 0.0;
+    for (int i = 0; i < num_regions; ++i) weights += std::pow(double(i + 1), double(balance));
+    if (weights > 2147483647.0) return fail(ctx, LULESH_ERR_ARG, "lulesh_set_regions: region weights overflow int");
+    // the run graph bakes in the kernel arguments: rebuild on next run
+    if (ctx->run_exec) { cudaGraphExecDestroy(ctx->run_exec); ctx->run_exec = nullptr; }
+    if (ctx->chunk_exec) { cudaGraphExecDestroy(ctx->chunk_exec); ctx->chunk_exec = nullptr; }
+    ctx->run_mode = 0;
+    if (num_regions == 0) {
+        ctx->regions.clear();
+        ctx->dom.mat_order = nullptr;
+        ctx->dom.reps = nullptr;
+        return LULESH_OK;
+    }
+    const long ne = ctx->ne;
+    region_numbers(ne, num_regions, balance, ctx->regions);
+    std::vector<int> reps(ne), order(ne);
+    for (long k = 0; k < ne; ++k) {
+        reps[k] = region_reps(ctx->regions[k] - 1, num_regions, cost);
+        order[k] = (int)k;
+    }
+    // costliest elements first, element order within a cost: warps see one
+    // repetition count and the longest ones start earliest
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return reps[a] > reps[b]; });
+    int rc;
+    if (!ctx->d_mat_order && (rc = dalloc(ctx, &ctx->d_mat_order, ne)) != LULESH_OK) return rc;
+    if (!ctx->d_reps && (rc = dalloc(ctx, &ctx->d_reps, ne)) != LULESH_OK) return rc;
+    CK(cudaMemcpyAsync(ctx->d_mat_order, order.data(), ne * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_reps, reps.data(), ne * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->dom.mat_order = ctx->d_mat_order;
+    ctx->dom.reps = ctx->d_reps;
+    return LULESH_OK;
+}
+
+int lulesh_get_regions(lulesh_ctx *ctx, int *reg_num_list)
+{
+    if (!ctx || !reg_num_list) return LULESH_ERR_ARG;
+    for (long k = 0; k < ctx->ne; ++k) reg_num_list[k] = ctx->regions.empty() ? 1 : ctx->regions[k];
     return LULESH_OK;
 }
 

@@ -124,19 +124,30 @@ __device__ __forceinline__ double sound_term(double pbvc, double e, double vv, d
 // element k (LULESH-OMP.cc:2369-2381, :2384-2782), given its monotonic-Q
 // terms; every loop of the reference there is element-local.  Writes
 // p, e, q, ss and v and returns the new sound speed.
+//
+// rep > 1 evaluates the EOS rep times from the same inputs, as LULESH 2.0
+// does for its costly regions (lulesh-2.0.3/lulesh.cc:2265-2323, called with
+// rep from :2410-2424): the results are those of one evaluation, and the
+// empty asm statements keep the compiler from merging or dropping the
+// repeated evaluations.
+__device__ __forceinline__ void opaque(double &v) { asm volatile("" : "+d"(v)); }
+__device__ __forceinline__ void consume(double v) { asm volatile("" ::"d"(v)); }
+
 __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalars *sc, double vnew,
-                                                  double qlin, double qquad)
+                                                  double qlin, double qquad, int rep = 1)
 {
     const lulesh_params &P = d.prm;
+    if (rep < 1) rep = 1;
     // CalcQForElems qstop test on the old q (:2369-2381)
-    const double q_old = d.q[k];
-    if (q_old > P.qstop) flag_error(sc, ERR_K3_QSTOP, k);
+    const double q_old_in = d.q[k];
+    if (q_old_in > P.qstop) flag_error(sc, ERR_K3_QSTOP, k);
 
     // ApplyMaterialPropertiesForElems (:2703-2761)
     const double eosvmin = P.eosvmin, eosvmax = P.eosvmax;
-    double vnewc = vnew;
-    if (eosvmin != 0. && vnewc < eosvmin) vnewc = eosvmin;
-    if (eosvmax != 0. && vnewc > eosvmax) vnewc = eosvmax;
+    double vnewc_in = vnew;
+    if (eosvmin != 0. && vnewc_in < eosvmin) vnewc_in = eosvmin;
+    if (eosvmax != 0. && vnewc_in > eosvmax) vnewc_in = eosvmax;
+    const double qlin_in = qlin, qquad_in = qquad;
     const double v_old = d.v[k];
     double vc = v_old;
     if (eosvmin != 0. && vc < eosvmin) vc = eosvmin;
@@ -144,58 +155,69 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
     if (vc <= 0.) flag_error(sc, ERR_K3_MATV, k);
 
     // EvalEOSForElems + CalcEnergyForElems (:2415-2701); work == 0
-    const double delvc = d.delv[k], e_old = d.e[k];
-    double p_old = d.p[k];
-    // __drcp_rn is the correctly rounded reciprocal: the bits of 1. / x
-    double compression = __drcp_rn(vnewc) - 1.;
-    const double vchalf = vnewc - delvc * .5;
-    double comp_half = __drcp_rn(vchalf) - 1.;
-    // vhalf = 1 / (1 + comp_half) (:2460), which is vchalf, vnewc or 1 in the
-    // three cases below; taken directly instead of through two divisions
-    double vhalf = vchalf;
-    if (eosvmin != 0. && vnewc <= eosvmin) {
-        comp_half = compression;
-        vhalf = vnewc;
-    }
-    if (eosvmax != 0. && vnewc >= eosvmax) {
-        p_old = 0.;
-        compression = 0.;
-        comp_half = 0.;
-        vhalf = 1.;
-    }
+    const double delvc_in = d.delv[k], e_old_in = d.e[k], p_old_in = d.p[k];
     const double rho0 = P.refdens;
     const bool unit_rho0 = (rho0 == 1.0);
     const double pbvc = 2.0 / 3.0;
-    const double emin = P.emin, e_cut = P.e_cut;
-    double bvc;
+    double p_new, e_new, q_new, bvc, ssn;
+    for (int j = 0; j < rep; ++j) {
+        double delvc = delvc_in, e_old = e_old_in, p_old = p_old_in, q_old = q_old_in, vnewc = vnewc_in;
+        double qlin = qlin_in, qquad = qquad_in;
+        if (rep > 1) {
+            opaque(delvc); opaque(e_old); opaque(p_old); opaque(q_old); opaque(vnewc);
+            opaque(qlin); opaque(qquad);
+        }
+        // __drcp_rn is the correctly rounded reciprocal: the bits of 1. / x
+        double compression = __drcp_rn(vnewc) - 1.;
+        const double vchalf = vnewc - delvc * .5;
+        double comp_half = __drcp_rn(vchalf) - 1.;
+        // vhalf = 1 / (1 + comp_half) (:2460), which is vchalf, vnewc or 1 in the
+        // three cases below; taken directly instead of through two divisions
+        double vhalf = vchalf;
+        if (eosvmin != 0. && vnewc <= eosvmin) {
+            comp_half = compression;
+            vhalf = vnewc;
+        }
+        if (eosvmax != 0. && vnewc >= eosvmax) {
+            p_old = 0.;
+            compression = 0.;
+            comp_half = 0.;
+            vhalf = 1.;
+        }
+        const double emin = P.emin, e_cut = P.e_cut;
 
-    double e_new = e_old - .5 * delvc * (p_old + q_old);
-    if (e_new < emin) e_new = emin;
-    const double p_half = eos_pressure(bvc, e_new, comp_half, vnewc, P);
-    double q_new = 0.;
-    if (!(delvc > 0.)) q_new = sound_term(pbvc, e_new, vhalf, bvc, p_half, rho0, unit_rho0) * qlin + qquad;
-    e_new = e_new + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (p_half + q_new));
-    if (fabs(e_new) < e_cut) e_new = 0.;
-    if (e_new < emin) e_new = emin;
+        e_new = e_old - .5 * delvc * (p_old + q_old);
+        if (e_new < emin) e_new = emin;
+        const double p_half = eos_pressure(bvc, e_new, comp_half, vnewc, P);
+        q_new = 0.;
+        if (!(delvc > 0.)) q_new = sound_term(pbvc, e_new, vhalf, bvc, p_half, rho0, unit_rho0) * qlin + qquad;
+        e_new = e_new + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (p_half + q_new));
+        if (fabs(e_new) < e_cut) e_new = 0.;
+        if (e_new < emin) e_new = emin;
 
-    double p_new = eos_pressure(bvc, e_new, compression, vnewc, P);
-    double q_tilde = 0.;
-    if (!(delvc > 0.)) q_tilde = sound_term(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0) * qlin + qquad;
-    const double sixth = 1.0 / 6.0;
-    e_new = e_new - (7.0 * (p_old + q_old) - 8.0 * (p_half + q_new) + (p_new + q_tilde)) * delvc * sixth;
-    if (fabs(e_new) < e_cut) e_new = 0.;
-    if (e_new < emin) e_new = emin;
+        p_new = eos_pressure(bvc, e_new, compression, vnewc, P);
+        double q_tilde = 0.;
+        if (!(delvc > 0.)) q_tilde = sound_term(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0) * qlin + qquad;
+        const double sixth = 1.0 / 6.0;
+        e_new = e_new - (7.0 * (p_old + q_old) - 8.0 * (p_half + q_new) + (p_new + q_tilde)) * delvc * sixth;
+        if (fabs(e_new) < e_cut) e_new = 0.;
+        if (e_new < emin) e_new = emin;
 
-    p_new = eos_pressure(bvc, e_new, compression, vnewc, P);
-    const double ssn = sound_term(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0);
-    if (delvc <= 0.) {
-        q_new = ssn * qlin + qquad;
-        if (fabs(q_new) < P.q_cut) q_new = 0.;
+        p_new = eos_pressure(bvc, e_new, compression, vnewc, P);
+        // CalcSoundSpeedForElems (:2543-2561) takes the last evaluation's
+        ssn = sound_term(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0);
+        if (delvc <= 0.) {
+            q_new = ssn * qlin + qquad;
+            if (fabs(q_new) < P.q_cut) q_new = 0.;
+        }
+        if (rep > 1) {
+            consume(p_new); consume(e_new); consume(q_new); consume(ssn);
+        }
     }
     d.p[k] = p_new;
     d.e[k] = e_new;
     d.q[k] = q_new;
-    d.ss[k] = ssn;     // CalcSoundSpeedForElems (:2543-2561)
+    d.ss[k] = ssn;
 
     // UpdateVolumesForElems (:2763-2782)
     double vt = vnew;

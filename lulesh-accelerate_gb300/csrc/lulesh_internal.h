@@ -75,6 +75,10 @@ struct LmeshFile {
 };
 
 double host_elem_volume(const double x[8], const double y[8], const double z[8]);
+// LULESH 2.0 region numbers (1..nr) of ne elements and the EOS repetitions
+// of region r (0-based)
+void region_numbers(long ne, int nr, int balance, std::vector<int> &reg);
+int region_reps(int r, int nr, int cost);
 void default_params(lulesh_params *p);
 
 // Everything one kernel launch needs, passed by value.
@@ -87,6 +91,9 @@ struct Dom {
     const int *corner_list;              // [8*ne] corner-major slots c*ne+e
     const unsigned char *node_bc;        // [nn]
     const int *lxim, *lxip, *letam, *letap, *lzetam, *lzetap, *elem_bc;
+    // LULESH 2.0 regions (null without): the material kernel visits elements
+    // in mat_order (grouped by cost) and evaluates the EOS reps[k] times
+    const int *mat_order, *reps;
     const double *volo, *elem_mass, *nodal_mass;
     // nodal state
     double *x, *y, *z, *xd, *yd, *zd;

@@ -388,6 +388,18 @@ int lulesh_mesh_sizes(int s, long *num_elem, long *num_node)
     return LULESH_OK;
 }
 
+int lulesh_region_numbers(long num_elem, int num_regions, int balance, int *reg_num_list)
+{
+    if (num_elem < 0 || num_regions < 1 || balance < 0 || (num_elem > 0 && !reg_num_list)) return LULESH_ERR_ARG;
+    double weights = 0.0;
+    for (int i = 0; i < num_regions; ++i) weights += std::pow(double(i + 1), double(balance));
+    if (weights > 2147483647.0) return LULESH_ERR_ARG;
+    std::vector<int> reg;
+    lulesh::region_numbers(num_elem, num_regions, balance, reg);
+    std::memcpy(reg_num_list, reg.data(), reg.size() * sizeof(int));
+    return LULESH_OK;
+}
+
 int lulesh_mesh_build(int s, int init_mode, lulesh_mesh_view *out)
 {
     if (!out || s < 1 || s > lulesh::kMaxEdge) return LULESH_ERR_ARG;
@@ -423,3 +435,100 @@ int lulesh_mesh_build(int s, int init_mode, lulesh_mesh_view *out)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------
+// LULESH 2.0 regions
+// ---------------------------------------------------------------------
+namespace lulesh {
+
+namespace {
+
+// The C library generator the reference seeds with srand(0) (glibc's
+// additive feedback generator: 34 words seeded by the Park-Miller LCG
+// x' = 16807 x mod (2^31 - 1), then r[i] = r[i-31] + r[i-3] mod 2^32 with
+// the first 310 outputs discarded, each output r >> 1).  Restated so that
+// the assignment does not depend on the host's rand() state.
+class CRand {
+  public:
+    explicit CRand(unsigned seed)
+    {
+        int32_t r = seed ? (int32_t)seed : 1;
+        w_[0] = (uint32_t)r;
+        for (int i = 1; i < 31; ++i) {
+            const int32_t hi = r / 127773, lo = r % 127773;
+            r = 16807 * lo - 2836 * hi;
+            if (r < 0) r += 2147483647;
+            w_[i] = (uint32_t)r;
+        }
+        for (int i = 31; i < 34; ++i) w_[i] = w_[i - 31];
+        n_ = 34;
+        for (int i = 34; i < 344; ++i) step();
+    }
+    int next() { return (int)(step() >> 1); }
+
+  private:
+    uint32_t step()
+    {
+        // ring of the last 34 words: r[n] = r[n-31] + r[n-3]
+        const uint32_t v = w_[(n_ - 31) % 34] + w_[(n_ - 3) % 34];
+        w_[n_ % 34] = v;
+        ++n_;
+        return v;
+    }
+    uint32_t w_[34];
+    long n_;
+};
+
+}  // namespace
+
+// Region number (1..nr) of each element, as CreateRegionIndexSets
+// (lulesh-2.0.3/lulesh-init.cc:377-486) assigns them on one rank: runs of
+// consecutive elements, each run's region drawn with weight (r+1)^balance
+// and never the previous run's region, each run's length drawn from the
+// reference's bin table.
+void region_numbers(long ne, int nr, int balance, std::vector<int> &reg)
+{
+    reg.assign(ne, 1);
+    if (nr <= 1) return;
+    CRand rnd(0);
+    std::vector<int> bin_end(nr);
+    int denom = 0;
+    for (int i = 0; i < nr; ++i) {
+        denom += (int)std::pow((double)(i + 1), (double)balance);
+        bin_end[i] = denom;
+    }
+    auto pick = [&]() {
+        const int v = rnd.next() % denom;
+        int i = 0;
+        while (v >= bin_end[i]) ++i;
+        return i % nr + 1;
+    };
+    long next = 0;
+    int last = -1;
+    while (next < ne) {
+        int region = pick();
+        while (region == last) region = pick();
+        const int bin = rnd.next() % 1000;
+        long len;
+        if (bin < 773) len = rnd.next() % 15 + 1;
+        else if (bin < 937) len = rnd.next() % 16 + 16;
+        else if (bin < 970) len = rnd.next() % 32 + 32;
+        else if (bin < 974) len = rnd.next() % 64 + 64;
+        else if (bin < 978) len = rnd.next() % 128 + 128;
+        else if (bin < 981) len = rnd.next() % 256 + 256;
+        else len = rnd.next() % 1537 + 512;
+        for (const long end = next + len; next < end && next < ne; ++next) reg[next] = region;
+        last = region;
+    }
+}
+
+// EOS evaluations per element of region r (0-based) of nr
+// (ApplyMaterialPropertiesForElems, lulesh-2.0.3/lulesh.cc:2410-2424).
+int region_reps(int r, int nr, int cost)
+{
+    if (r < nr / 2) return 1;
+    if (r < nr - (nr + 15) / 20) return 1 + cost;
+    return 10 * (1 + cost);
+}
+
+}  // namespace lulesh

@@ -334,7 +334,7 @@ __device__ __forceinline__ void elem_material_fp64(const Dom &d, int k, DevScala
             d.qq[k] = qquad;
         }
 
-        const double ssn = material_update(d, k, sc, vnew, qlin, qquad);
+        const double ssn = material_update(d, k, sc, vnew, qlin, qquad, d.reps ? __ldg(d.reps + k) : 1);
 
         if (kConstraints) constraint_keys(ssn, vdov, d.arealg[k], P, kc, kh);
     }
@@ -343,9 +343,14 @@ __device__ __forceinline__ void elem_material_fp64(const Dom &d, int k, DevScala
 template <bool kConstraints>
 __global__ void __launch_bounds__(kBlockElem) k_elem_material(const __grid_constant__ Dom d)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long kc = ~0ULL, kh = ~0ULL;
-    if (k < d.ne && !skip_step(d)) elem_material_fp64<kConstraints>(d, k, d.sc, kc, kh);
+    if (t < d.ne && !skip_step(d)) {
+        // with regions, threads take elements in cost-grouped order (the
+        // reference's region element lists, lulesh-2.0.3/lulesh.cc:2410-2424)
+        const int k = d.mat_order ? __ldg(d.mat_order + t) : t;
+        elem_material_fp64<kConstraints>(d, k, d.sc, kc, kh);
+    }
     if (kConstraints) block_min_publish(kc, kh, d.sc);
 }
 

@@ -409,7 +409,7 @@ __device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScal
             d.ql[k] = qlin;
             d.qq[k] = qquad;
         }
-        const double ssn = material_update(d, k, sc, vnew, qlin, qquad);
+        const double ssn = material_update(d, k, sc, vnew, qlin, qquad, d.reps ? __ldg(d.reps + k) : 1);
         if (kConstraints) constraint_keys(ssn, vdov, d.arealg[k], P, kc, kh);
     }
 }
@@ -417,9 +417,12 @@ __device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScal
 template <bool kConstraints>
 __global__ void __launch_bounds__(kBlockElem) k_elem_material_split(const __grid_constant__ Dom d)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long kc = ~0ULL, kh = ~0ULL;
-    if (k < d.ne && !skip_step(d)) elem_material_split<kConstraints>(d, k, d.sc, kc, kh);
+    if (t < d.ne && !skip_step(d)) {
+        const int k = d.mat_order ? __ldg(d.mat_order + t) : t;   // cost-grouped order with regions
+        elem_material_split<kConstraints>(d, k, d.sc, kc, kh);
+    }
     if (kConstraints) block_min_publish(kc, kh, d.sc);
 }
 
