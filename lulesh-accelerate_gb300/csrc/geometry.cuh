@@ -19,35 +19,6 @@ __device__ __forceinline__ void jac_column(const T c[8], T &xi, T &et, T &ze)
     ze = T(.125) * (((d60 + d53) + d71) + d42);
 }
 
-// CalcElemShapeFunctionDerivatives (LULESH-OMP.cc:619-706): B for corners
-// 0..3 (4..7 are their negatives) and the Jacobian volume.
-__device__ __forceinline__ void shape_derivs4(const double x[8], const double y[8], const double z[8],
-                                              double b[3][4], double &volume)
-{
-    double a[3], t[3], c[3];
-    jac_column(x, a[0], t[0], c[0]);
-    jac_column(y, a[1], t[1], c[1]);
-    jac_column(z, a[2], t[2], c[2]);
-    double cxi[3], cet[3], cze[3];
-    cxi[0] = (t[1] * c[2]) - (t[2] * c[1]);
-    cxi[1] = (t[2] * c[0]) - (t[0] * c[2]);
-    cxi[2] = (t[0] * c[1]) - (t[1] * c[0]);
-    cet[0] = (a[2] * c[1]) - (a[1] * c[2]);
-    cet[1] = (a[0] * c[2]) - (a[2] * c[0]);
-    cet[2] = (a[1] * c[0]) - (a[0] * c[1]);
-    cze[0] = (a[1] * t[2]) - (a[2] * t[1]);
-    cze[1] = (a[2] * t[0]) - (a[0] * t[2]);
-    cze[2] = (a[0] * t[1]) - (a[1] * t[0]);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        b[d][0] = ((-cxi[d]) - cet[d]) - cze[d];
-        b[d][1] = (cxi[d] - cet[d]) - cze[d];
-        b[d][2] = (cxi[d] + cet[d]) - cze[d];
-        b[d][3] = ((-cxi[d]) + cet[d]) - cze[d];
-    }
-    volume = 8.0 * ((t[0] * cet[0] + t[1] * cet[1]) + t[2] * cet[2]);
-}
-
 // Jacobian volume only (the determinant IntegrateStressForElems checks).
 template <typename T>
 __device__ __forceinline__ T jacobian_volume(const T x[8], const T y[8], const T z[8])
@@ -60,48 +31,6 @@ __device__ __forceinline__ T jacobian_volume(const T x[8], const T y[8], const T
     const T cet1 = (a[0] * c[2]) - (a[2] * c[0]);
     const T cet2 = (a[1] * c[0]) - (a[0] * c[1]);
     return T(8.0) * ((t[0] * cet0 + t[1] * cet1) + t[2] * cet2);
-}
-
-// CalcElemNodeNormals + SumElemFaceNormal (LULESH-OMP.cc:708-799).  The six
-// faces are visited in the reference's order; each corner accumulates the
-// quarter-area vectors of its three faces in that order.
-__device__ __forceinline__ void face_area(const double x[8], const double y[8], const double z[8],
-                                          int n0, int n1, int n2, int n3,
-                                          double &ax, double &ay, double &az)
-{
-    const double bx0 = 0.5 * (((x[n3] + x[n2]) - x[n1]) - x[n0]);
-    const double by0 = 0.5 * (((y[n3] + y[n2]) - y[n1]) - y[n0]);
-    const double bz0 = 0.5 * (((z[n3] + z[n2]) - z[n1]) - z[n0]);
-    const double bx1 = 0.5 * (((x[n2] + x[n1]) - x[n3]) - x[n0]);
-    const double by1 = 0.5 * (((y[n2] + y[n1]) - y[n3]) - y[n0]);
-    const double bz1 = 0.5 * (((z[n2] + z[n1]) - z[n3]) - z[n0]);
-    ax = 0.25 * (by0 * bz1 - bz0 * by1);
-    ay = 0.25 * (bz0 * bx1 - bx0 * bz1);
-    az = 0.25 * (bx0 * by1 - by0 * bx1);
-}
-
-__device__ __forceinline__ void node_normals(double pf[3][8], const double x[8], const double y[8],
-                                             const double z[8])
-{
-    double a[6][3];
-    face_area(x, y, z, 0, 1, 2, 3, a[0][0], a[0][1], a[0][2]);
-    face_area(x, y, z, 0, 4, 5, 1, a[1][0], a[1][1], a[1][2]);
-    face_area(x, y, z, 1, 5, 6, 2, a[2][0], a[2][1], a[2][2]);
-    face_area(x, y, z, 2, 6, 7, 3, a[3][0], a[3][1], a[3][2]);
-    face_area(x, y, z, 3, 7, 4, 0, a[4][0], a[4][1], a[4][2]);
-    face_area(x, y, z, 4, 7, 6, 5, a[5][0], a[5][1], a[5][2]);
-    // faces touching each corner, ascending (= accumulation order)
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        pf[d][0] = (a[0][d] + a[1][d]) + a[4][d];
-        pf[d][1] = (a[0][d] + a[1][d]) + a[2][d];
-        pf[d][2] = (a[0][d] + a[2][d]) + a[3][d];
-        pf[d][3] = (a[0][d] + a[3][d]) + a[4][d];
-        pf[d][4] = (a[1][d] + a[4][d]) + a[5][d];
-        pf[d][5] = (a[1][d] + a[2][d]) + a[5][d];
-        pf[d][6] = (a[2][d] + a[3][d]) + a[5][d];
-        pf[d][7] = (a[3][d] + a[4][d]) + a[5][d];
-    }
 }
 
 // Node normals from the face diagonals, for the split-precision step.  For a
@@ -183,32 +112,6 @@ __device__ __forceinline__ void volume_derivative(T dvdx[8], T dvdy[8], T dvdz[8
     volu_der(x, y, z, 4, 7, 6, 1, 0, 2, dvdx[5], dvdy[5], dvdz[5]);
     volu_der(x, y, z, 5, 4, 7, 2, 1, 3, dvdx[6], dvdy[6], dvdz[6]);
     volu_der(x, y, z, 6, 5, 4, 3, 2, 0, dvdx[7], dvdy[7], dvdz[7]);
-}
-
-// CalcElemVolume (LULESH-OMP.cc:1706-1790).
-__device__ __forceinline__ double elem_volume(const double x[8], const double y[8], const double z[8])
-{
-    const double twelveth = 1.0 / 12.0;
-    const double dx61 = x[6] - x[1], dy61 = y[6] - y[1], dz61 = z[6] - z[1];
-    const double dx70 = x[7] - x[0], dy70 = y[7] - y[0], dz70 = z[7] - z[0];
-    const double dx63 = x[6] - x[3], dy63 = y[6] - y[3], dz63 = z[6] - z[3];
-    const double dx20 = x[2] - x[0], dy20 = y[2] - y[0], dz20 = z[2] - z[0];
-    const double dx50 = x[5] - x[0], dy50 = y[5] - y[0], dz50 = z[5] - z[0];
-    const double dx64 = x[6] - x[4], dy64 = y[6] - y[4], dz64 = z[6] - z[4];
-    const double dx31 = x[3] - x[1], dy31 = y[3] - y[1], dz31 = z[3] - z[1];
-    const double dx72 = x[7] - x[2], dy72 = y[7] - y[2], dz72 = z[7] - z[2];
-    const double dx43 = x[4] - x[3], dy43 = y[4] - y[3], dz43 = z[4] - z[3];
-    const double dx57 = x[5] - x[7], dy57 = y[5] - y[7], dz57 = z[5] - z[7];
-    const double dx14 = x[1] - x[4], dy14 = y[1] - y[4], dz14 = z[1] - z[4];
-    const double dx25 = x[2] - x[5], dy25 = y[2] - y[5], dz25 = z[2] - z[5];
-#define LULESH_TRIPLE(x1, y1, z1, x2, y2, z2, x3, y3, z3) \
-    ((x1) * ((y2) * (z3) - (z2) * (y3)) + (x2) * ((z1) * (y3) - (y1) * (z3)) + (x3) * ((y1) * (z2) - (z1) * (y2)))
-    const double vol =
-        LULESH_TRIPLE(dx31 + dx72, dx63, dx20, dy31 + dy72, dy63, dy20, dz31 + dz72, dz63, dz20) +
-        LULESH_TRIPLE(dx43 + dx57, dx64, dx70, dy43 + dy57, dy64, dy70, dz43 + dz57, dz64, dz70) +
-        LULESH_TRIPLE(dx14 + dx25, dx61, dx50, dy14 + dy25, dy61, dy50, dz14 + dz25, dz61, dz50);
-#undef LULESH_TRIPLE
-    return vol * twelveth;
 }
 
 // AreaFace (LULESH-OMP.cc:1799-1819).

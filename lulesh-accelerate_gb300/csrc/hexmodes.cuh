@@ -85,16 +85,6 @@ __device__ __forceinline__ V3<T> mode(const T mx[7], const T my[7], const T mz[7
     return {mx[i], my[i], mz[i]};
 }
 
-// 64 x volume of the trilinear hexahedron.
-template <typename T>
-__device__ __forceinline__ T volume64(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3, const V3<T> &M4,
-                                      const V3<T> &M5, const V3<T> &M6)
-{
-    const T third = T(1.0) / T(3.0);
-    const T bil = dot3(M4, cross3(M2, M6)) + dot3(M5, cross3(M6, M3)) + dot3(M1, cross3(M4, M5));
-    return dot3(M1, cross3(M2, M3)) + bil * third;
-}
-
 // Corner values of sum_{i=1..6} s_i(c) q_i (inverse Walsh transform with
 // the constant and xi eta zeta modes zero), 20 additions.
 template <typename T>
@@ -160,77 +150,70 @@ __device__ __forceinline__ void force_geometry64(const V3<T> &M1, const V3<T> &M
     pf[3] = {-(t2.x + X3.x), -(t2.y + X3.y), -(t2.z + X3.z)};   // (-,+,-)
 }
 
-// 64 x the volume derivative of each corner, D[c] = dV/dx_c * 64.
+// The six cross products of the modes that the volume, the node normals, the
+// Q gradients and the face areas share: c23 = M2xM3, c31 = M3xM1, c12 = M1xM2,
+// c45 = M4xM5, c64 = M6xM4, c56 = M5xM6.
 template <typename T>
-__device__ __forceinline__ void volume_derivative64(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
-                                                    const V3<T> &M4, const V3<T> &M5, const V3<T> &M6,
-                                                    T dx[8], T dy[8], T dz[8])
+struct ModeCrosses {
+    V3<T> c23, c31, c12, c45, c64, c56;
+};
+
+template <typename T>
+__device__ __forceinline__ ModeCrosses<T> mode_crosses(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
+                                                       const V3<T> &M4, const V3<T> &M5, const V3<T> &M6)
+{
+    return {cross3(M2, M3), cross3(M3, M1), cross3(M1, M2), cross3(M4, M5), cross3(M6, M4), cross3(M5, M6)};
+}
+
+// 64 x volume through the shared crosses: the bilinear terms of volume64 are
+// scalar triple products, M4.(M2xM6) = M2.(M6xM4) and M5.(M6xM3) = M3.(M5xM6).
+template <typename T>
+__device__ __forceinline__ T volume64_shared(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
+                                             const ModeCrosses<T> &C)
 {
     const T third = T(1.0) / T(3.0);
-    auto add3 = [](const V3<T> &a, const V3<T> &b, T s) {
-        return V3<T>{a.x + b.x * s, a.y + b.y * s, a.z + b.z * s};
-    };
-    auto sum3 = [](const V3<T> &a, const V3<T> &b, T s) {
-        return V3<T>{(a.x + b.x) * s, (a.y + b.y) * s, (a.z + b.z) * s};
-    };
-    const V3<T> W1 = add3(cross3(M2, M3), cross3(M4, M5), third);
-    const V3<T> W2 = add3(cross3(M3, M1), cross3(M6, M4), third);
-    const V3<T> W3 = add3(cross3(M1, M2), cross3(M5, M6), third);
-    const V3<T> W4 = sum3(cross3(M2, M6), cross3(M5, M1), third);
-    const V3<T> W5 = sum3(cross3(M6, M3), cross3(M1, M4), third);
-    const V3<T> W6 = sum3(cross3(M4, M2), cross3(M3, M5), third);
-    inv_walsh6(W1.x, W2.x, W3.x, W4.x, W5.x, W6.x, dx);
-    inv_walsh6(W1.y, W2.y, W3.y, W4.y, W5.y, W6.y, dy);
-    inv_walsh6(W1.z, W2.z, W3.z, W4.z, W5.z, W6.z, dz);
+    return dot3(M1, C.c23) + ((dot3(M2, C.c64) + dot3(M3, C.c56)) + dot3(M1, C.c45)) * third;
 }
 
-// Unscaled node normals: corner sums of v x u over the three faces of each
-// corner, u and v the face diagonals (8 x the reference's node normals,
-// :708-799).
+// 64 x the largest |u x v|^2 over the six faces (u, v the face diagonals),
+// through the modes.  On the face xi = s the surface is bilinear in (eta,
+// zeta) with edge vectors (M2 + s M4)/8 and (M3 + s M5)/8, and u x v is 8
+// times their cross product: (X1 + s Y1)/8 with X1 = M2xM3 + M4xM5 and
+// Y1 = M2xM5 + M4xM3; likewise X2 = M3xM1 + M6xM4, Y2 = M6xM1 + M3xM4 for
+// eta = s and X3 = M1xM2 + M5xM6, Y3 = M1xM6 + M5xM2 for zeta = s.  The
+// larger of the two faces of a direction is |X|^2 + |Y|^2 + 2|X.Y|.
 template <typename T>
-__device__ __forceinline__ void node_normals8(T pf[3][8], const T x[8], const T y[8], const T z[8])
+__device__ __forceinline__ T max_face_cross2_64(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
+                                                const V3<T> &M4, const V3<T> &M5, const V3<T> &M6,
+                                                const ModeCrosses<T> &C)
 {
-    T a[6][3];
-    const int f[6][4] = {{0, 1, 2, 3}, {0, 4, 5, 1}, {1, 5, 6, 2}, {2, 6, 7, 3}, {3, 7, 4, 0}, {4, 7, 6, 5}};
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        const int n0 = f[i][0], n1 = f[i][1], n2 = f[i][2], n3 = f[i][3];
-        const T ux = x[n2] - x[n0], uy = y[n2] - y[n0], uz = z[n2] - z[n0];
-        const T vx = x[n3] - x[n1], vy = y[n3] - y[n1], vz = z[n3] - z[n1];
-        a[i][0] = vy * uz - vz * uy;
-        a[i][1] = vz * ux - vx * uz;
-        a[i][2] = vx * uy - vy * ux;
-    }
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        pf[d][0] = (a[0][d] + a[1][d]) + a[4][d];
-        pf[d][1] = (a[0][d] + a[1][d]) + a[2][d];
-        pf[d][2] = (a[0][d] + a[2][d]) + a[3][d];
-        pf[d][3] = (a[0][d] + a[3][d]) + a[4][d];
-        pf[d][4] = (a[1][d] + a[4][d]) + a[5][d];
-        pf[d][5] = (a[1][d] + a[2][d]) + a[5][d];
-        pf[d][6] = (a[2][d] + a[3][d]) + a[5][d];
-        pf[d][7] = (a[3][d] + a[4][d]) + a[5][d];
-    }
+    const V3<T> a = cross3(M3, M4), b = cross3(M2, M5), c = cross3(M6, M1);
+    auto pair = [](const V3<T> &p, const V3<T> &q, const V3<T> &r, const V3<T> &t, T sy) {
+        const V3<T> X{p.x + q.x, p.y + q.y, p.z + q.z};
+        const V3<T> Y{r.x + sy * t.x, r.y + sy * t.y, r.z + sy * t.z};
+        return (dot3(X, X) + dot3(Y, Y)) + T(2.0) * fabs(dot3(X, Y));
+    };
+    const T f1 = pair(C.c23, C.c45, b, a, T(-1.0));   // Y1 = b - a
+    const T f2 = pair(C.c31, C.c64, c, a, T(1.0));    // Y2 = c + a
+    const T f3 = pair(C.c12, C.c56, c, b, T(1.0));    // |Y3| = |c + b|
+    return fmax(fmax(f1, f2), f3);
 }
 
-// Largest |u x v|^2 over the six faces, u and v the face diagonals: the
-// reference's AreaFace (:1799-1819) is |f|^2|g|^2 - (f.g)^2 with f = u - v,
-// g = u + v, which equals 4|u x v|^2 (Lagrange's identity).
+// The strain rate tr(grad v) at the half step (CalcElemVelocityGrandient +
+// trace, LULESH-OMP.cc:1864-1925, 1975-2020): the half-step Jacobian has
+// columns (M - dt2 Mv)/8 for the position modes M1..M3 and velocity modes
+// V1..V3, and the trace is sum(cofactor . velocity mode) / det.
 template <typename T>
-__device__ __forceinline__ T max_face_cross2(const T x[8], const T y[8], const T z[8])
+__device__ __forceinline__ T strain_rate(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3, const V3<T> &V1,
+                                         const V3<T> &V2, const V3<T> &V3m, T dt2)
 {
-    const int f[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
-    T m = T(0.0);
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        const int a = f[i][0], b = f[i][1], c = f[i][2], d = f[i][3];
-        const V3<T> u{x[c] - x[a], y[c] - y[a], z[c] - z[a]};
-        const V3<T> v{x[d] - x[b], y[d] - y[b], z[d] - z[b]};
-        const V3<T> w = cross3(u, v);
-        m = fmax(dot3(w, w), m);
-    }
-    return m;
+    const V3<T> A{M1.x - dt2 * V1.x, M1.y - dt2 * V1.y, M1.z - dt2 * V1.z};
+    const V3<T> B{M2.x - dt2 * V2.x, M2.y - dt2 * V2.y, M2.z - dt2 * V2.z};
+    const V3<T> C{M3.x - dt2 * V3m.x, M3.y - dt2 * V3m.y, M3.z - dt2 * V3m.z};
+    const V3<T> cxi = cross3(B, C), cet = cross3(C, A), cze = cross3(A, B);
+    const T num = (cxi.x * V1.x + cet.x * V2.x + cze.x * V3m.x) + (cxi.y * V1.y + cet.y * V2.y + cze.y * V3m.y) +
+                  (cxi.z * V1.z + cet.z * V2.z + cze.z * V3m.z);
+    return num / dot3(B, cet);
 }
 
 }  // namespace lulesh

@@ -236,14 +236,17 @@ __device__ __forceinline__ void elem_kinematics_fp64(const Dom &d, int k, DevSca
     const V3<double> V1{vx[0], vy[0], vz[0]}, V2{vx[1], vy[1], vz[1]}, V3v{vx[2], vy[2], vz[2]};
 
     // CalcKinematicsForElems, volume part (:1950-1964)
+    const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
+    const ModeCrosses<double> X = mode_crosses(M1, M2, M3, M4, M5, M6);
     const double volo = d.volo[k];
-    const double volume =
-        volume64(M1, M2, M3, mode(mx, my, mz, 3), mode(mx, my, mz, 4), mode(mx, my, mz, 5)) * (1.0 / 64.0);
+    const double vol64 = volume64_shared(M1, M2, M3, X);
+    const double volume = vol64 * (1.0 / 64.0);
     const double rel = volume / volo;
     d.vnew[k] = rel;
     d.delv[k] = rel - d.v[k];
-    // CalcElemCharacteristicLength (:1821-1862): 4V / sqrt(max 4|u x v|^2)
-    d.arealg[k] = (2.0 * volume) * rsqrt(max_face_cross2(x, y, z));
+    // CalcElemCharacteristicLength (:1821-1862): 4V / sqrt(max AreaFace) with
+    // AreaFace = 4|u x v|^2 = (64 |u x v|^2) / 16
+    d.arealg[k] = (0.25 * vol64) * rsqrt(max_face_cross2_64(M1, M2, M3, M4, M5, M6, X));
     if (rel <= 0.0) flag_error(sc, ERR_K3_VNEW, k);
 
     // CalcMonotonicQGradientsForElems (:2034-2180): the logical differences
@@ -254,7 +257,7 @@ __device__ __forceinline__ void elem_kinematics_fp64(const Dom &d, int k, DevSca
         const double vol = volo * rel;
         const double norm = __drcp_rn(vol + ptiny);
         const double vscale = 0.015625 * norm;           // (1/16) (1/4) norm
-        const V3<double> Az = cross3(M1, M2), Ax = cross3(M2, M3), Ae = cross3(M3, M1);
+        const V3<double> &Az = X.c12, &Ax = X.c23, &Ae = X.c31;
         d.delx_zeta[k] = vol * rsqrt(0.00390625 * dot3(Az, Az) + ptiny);
         d.delv_zeta[k] = vscale * dot3(Az, V3v);
         d.delx_xi[k] = vol * rsqrt(0.00390625 * dot3(Ax, Ax) + ptiny);
@@ -263,18 +266,8 @@ __device__ __forceinline__ void elem_kinematics_fp64(const Dom &d, int k, DevSca
         d.delv_eta[k] = vscale * dot3(Ae, V2);
     }
 
-    // CalcKinematicsForElems, strain-rate part (:1975-2020): the Jacobian at
-    // the half step has columns (M - dt/2 Mv)/8; tr(grad v) = sum over
-    // cofactors x velocity modes / det.
-    const double dt2 = 0.5 * sc->deltatime;
-    const V3<double> A{M1.x - dt2 * V1.x, M1.y - dt2 * V1.y, M1.z - dt2 * V1.z};
-    const V3<double> T{M2.x - dt2 * V2.x, M2.y - dt2 * V2.y, M2.z - dt2 * V2.z};
-    const V3<double> C{M3.x - dt2 * V3v.x, M3.y - dt2 * V3v.y, M3.z - dt2 * V3v.z};
-    const V3<double> cxi = cross3(T, C), cet = cross3(C, A), cze = cross3(A, T);
-    const double num = (cxi.x * vx[0] + cet.x * vx[1] + cze.x * vx[2]) +
-                       (cxi.y * vy[0] + cet.y * vy[1] + cze.y * vy[2]) +
-                       (cxi.z * vz[0] + cet.z * vz[1] + cze.z * vz[2]);
-    d.vdov[k] = num / dot3(T, cet);
+    // CalcKinematicsForElems, strain-rate part (:1975-2020)
+    d.vdov[k] = strain_rate(M1, M2, M3, V1, V2, V3v, 0.5 * sc->deltatime);
 }
 
 __global__ void __launch_bounds__(kBlockElem) k_elem_kinematics(const __grid_constant__ Dom d)

@@ -24,6 +24,7 @@
 #include "lulesh_internal.h"
 #include "kernels.h"
 #include "geometry.cuh"
+#include "hexmodes.cuh"
 #include "common.cuh"
 #include "batch_kernels.cuh"
 
@@ -270,38 +271,31 @@ __device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevSc
     int nl[8];
     load_nodelist(d.nodelist, k, nl);
 
-    // FP64: relative volume and its change (CalcKinematicsForElems :1950-1958)
+    // FP64: relative volume and the half-step strain rate through the Walsh
+    // modes of the corner coordinates and velocities (CalcKinematicsForElems
+    // :1950-1958, :1975-2020; the identities of hexmodes.cuh)
     const double volo = d.volo[k];
     double volume, vdov;
     {
-        double X[8], Y[8], Z[8], U[8], V[8], W[8];
-        gather8(d.x, nl, X);
-        gather8(d.y, nl, Y);
-        gather8(d.z, nl, Z);
-        volume = elem_volume(X, Y, Z);
-        // FP64: the strain rate at the half step (:1975-2020)
-        gather8(d.xd, nl, U);
-        gather8(d.yd, nl, V);
-        gather8(d.zd, nl, W);
-        const double dt2 = 0.5 * sc->deltatime;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            X[j] -= dt2 * U[j];
-            Y[j] -= dt2 * V[j];
-            Z[j] -= dt2 * W[j];
-        }
-        double b[3][4], detJ;
-        shape_derivs4(X, Y, Z, b, detJ);
-        const double inv = 1.0 / detJ;
-        const double *vel[3] = {U, V, W};
-        double dd[3];
-#pragma unroll
-        for (int dim = 0; dim < 3; ++dim) {
-            const double *u = vel[dim];
-            dd[dim] = inv * (((b[dim][0] * (u[0] - u[6]) + b[dim][1] * (u[1] - u[7])) +
-                              b[dim][2] * (u[2] - u[4])) + b[dim][3] * (u[3] - u[5]));
-        }
-        vdov = (dd[0] + dd[1]) + dd[2];
+        double u[8], mx[7], my[7], mz[7];
+        gather8(d.x, nl, u);
+        walsh8(u, mx);
+        gather8(d.y, nl, u);
+        walsh8(u, my);
+        gather8(d.z, nl, u);
+        walsh8(u, mz);
+        const V3<double> M1 = mode(mx, my, mz, 0), M2 = mode(mx, my, mz, 1), M3 = mode(mx, my, mz, 2);
+        const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
+        volume = volume64_shared(M1, M2, M3, mode_crosses(M1, M2, M3, M4, M5, M6)) * (1.0 / 64.0);
+        double vx[3], vy[3], vz[3];
+        gather8(d.xd, nl, u);
+        walsh_linear(u, vx);
+        gather8(d.yd, nl, u);
+        walsh_linear(u, vy);
+        gather8(d.zd, nl, u);
+        walsh_linear(u, vz);
+        vdov = strain_rate(M1, M2, M3, V3<double>{vx[0], vy[0], vz[0]}, V3<double>{vx[1], vy[1], vz[1]},
+                           V3<double>{vx[2], vy[2], vz[2]}, 0.5 * sc->deltatime);
     }
     const double rel = volume / volo;
     d.vnew[k] = rel;
