@@ -87,6 +87,66 @@ __device__ __forceinline__ void rel8(const float2 *__restrict__ f, const int nl[
     }
 }
 
+// ---- compensated FP32 sums of hi/lo pairs ---------------------------------
+// A value carried as an unevaluated sum hi + lo of two floats.
+struct DF {
+    float hi, lo;
+};
+
+// b - a for hi/lo pairs: Knuth's two-sum gives the exact difference of the
+// hi words as s + e; the lo words' difference is added to e.
+__device__ __forceinline__ DF df_diff(float2 b, float2 a)
+{
+    const float s = b.x - a.x;
+    const float bb = s - b.x;
+    const float e = (b.x - (s - bb)) - (a.x + bb);
+    return {s, e + (b.y - a.y)};
+}
+
+// a + b + c + d: exact two-sums on the hi words, the rest summed in FP32.
+__device__ __forceinline__ DF df_sum4(DF a, DF b, DF c, DF d)
+{
+    float s = a.hi, err = 0.f;
+    const float h[3] = {b.hi, c.hi, d.hi};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float t = s + h[i];
+        const float bb = t - s;
+        err += (s - (t - bb)) + (h[i] - bb);
+        s = t;
+    }
+    return {s, ((a.lo + b.lo) + (c.lo + d.lo)) + err};
+}
+
+__device__ __forceinline__ DF df_neg(DF a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ double df_value(DF a) { return f2d(a.hi) + f2d(a.lo); }
+
+// The Walsh modes M1..M6 of one coordinate of the 8 corners, from hi/lo
+// pairs, in FP64.  Every mode but the constant one is a signed sum of four
+// edge differences (M1 = a+b+c+d, M4 = -a+b-c+d, M5 = -a-b+c+d over the xi
+// edges a..d; M2 = p+q+r+t, M6 = -p-q+r+t over the eta edges; M3 over the
+// zeta edges), so the sums run on small, exactly formed differences in
+// compensated FP32 and only the six results are converted and added in
+// FP64.  With linear_only, M1..M3 alone.
+template <bool kLinearOnly>
+__device__ __forceinline__ void df_modes(const float2 *__restrict__ f, const int nl[8], double m[6])
+{
+    float2 c[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) c[i] = __ldg(f + nl[i]);
+    const DF a = df_diff(c[1], c[0]), b = df_diff(c[2], c[3]), cc = df_diff(c[5], c[4]), dd = df_diff(c[6], c[7]);
+    const DF p = df_diff(c[3], c[0]), q = df_diff(c[2], c[1]), r = df_diff(c[7], c[4]), t = df_diff(c[6], c[5]);
+    const DF u = df_diff(c[4], c[0]), v = df_diff(c[5], c[1]), w = df_diff(c[6], c[2]), z = df_diff(c[7], c[3]);
+    m[0] = df_value(df_sum4(a, b, cc, dd));
+    m[1] = df_value(df_sum4(p, q, r, t));
+    m[2] = df_value(df_sum4(u, v, w, z));
+    if (!kLinearOnly) {
+        m[3] = df_value(df_sum4(df_neg(a), b, df_neg(cc), dd));
+        m[4] = df_value(df_sum4(df_neg(a), df_neg(b), cc, dd));
+        m[5] = df_value(df_sum4(df_neg(p), df_neg(q), r, t));
+    }
+}
+
 // FP64 state -> hi/lo pairs and reciprocal masses (after any host upload).
 __global__ void __launch_bounds__(kBlockNode) k_split_sync(const __grid_constant__ Dom d)
 {
@@ -273,27 +333,23 @@ __device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevSc
 
     // FP64: relative volume and the half-step strain rate through the Walsh
     // modes of the corner coordinates and velocities (CalcKinematicsForElems
-    // :1950-1958, :1975-2020; the identities of hexmodes.cuh)
+    // :1950-1958, :1975-2020; the identities of hexmodes.cuh).  The modes
+    // come from the hi/lo pairs by compensated FP32 edge sums (df_modes);
+    // cross products, volume, strain rate and the divisions are FP64.
     const double volo = d.volo[k];
     double volume, vdov;
     {
-        double u[8], mx[7], my[7], mz[7];
-        gather8(d.x, nl, u);
-        walsh8(u, mx);
-        gather8(d.y, nl, u);
-        walsh8(u, my);
-        gather8(d.z, nl, u);
-        walsh8(u, mz);
+        double mx[6], my[6], mz[6];
+        df_modes<false>(d.xs, nl, mx);
+        df_modes<false>(d.ys, nl, my);
+        df_modes<false>(d.zs, nl, mz);
         const V3<double> M1 = mode(mx, my, mz, 0), M2 = mode(mx, my, mz, 1), M3 = mode(mx, my, mz, 2);
         const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
         volume = volume64_shared(M1, M2, M3, mode_crosses(M1, M2, M3, M4, M5, M6)) * (1.0 / 64.0);
-        double vx[3], vy[3], vz[3];
-        gather8(d.xd, nl, u);
-        walsh_linear(u, vx);
-        gather8(d.yd, nl, u);
-        walsh_linear(u, vy);
-        gather8(d.zd, nl, u);
-        walsh_linear(u, vz);
+        double vx[6], vy[6], vz[6];
+        df_modes<true>(d.xds, nl, vx);
+        df_modes<true>(d.yds, nl, vy);
+        df_modes<true>(d.zds, nl, vz);
         vdov = strain_rate(M1, M2, M3, V3<double>{vx[0], vy[0], vz[0]}, V3<double>{vx[1], vy[1], vz[1]},
                            V3<double>{vx[2], vy[2], vz[2]}, 0.5 * sc->deltatime);
     }
