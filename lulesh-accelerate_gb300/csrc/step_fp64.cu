@@ -62,7 +62,7 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
     const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
     double dvdx[8], dvdy[8], dvdz[8];
     V3<double> pf[4];
-    force_geometry64(M1, M2, M3, M4, M5, M6, dvdx, dvdy, dvdz, pf);   // 64 x dV/dx, 64 x normals
+    force_geometry(M1, M2, M3, M4, M5, M6, dvdx, dvdy, dvdz, pf);   // 192 x dV/dx, 64 x normals
 
     // IntegrateStressForElems (LULESH-OMP.cc:853-903): sig = -p - q and the
     // corner force -sig * (area-weighted node normal); corners 4..7 carry
@@ -104,8 +104,8 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
     // CalcFBHourglassForceForElems (:1291-1473): hourgam = gamma -
     // volinv * (dV/dx . hourmod), with hourmod the gamma projections of the
     // coordinates (modes M6, M5, M4, M7).
-    const double r = rcbrt(determ);                       // determ^(-1/3)
-    const double volinv64 = (r * r * r) * (1.0 / 64.0);   // the 1/64 of the derivative
+    const double r = rcbrt(determ);                         // determ^(-1/3)
+    const double volinv192 = (r * r * r) * (1.0 / 192.0);   // the 1/192 of the derivative
     double hg[8][4];
     {
         const V3<double> M7 = mode(mx, my, mz, 6);
@@ -117,10 +117,12 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
             {-1.,  1., -1.,  1.,  1., -1.,  1., -1.}};
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            const double hx = volinv64 * H[m].x, hy = volinv64 * H[m].y, hz = volinv64 * H[m].z;
+            // the projection enters negated, so gamma is the addend of the
+            // three fused multiply-adds
+            const double hx = -(volinv192 * H[m].x), hy = -(volinv192 * H[m].y), hz = -(volinv192 * H[m].z);
 #pragma unroll
             for (int c = 0; c < 8; ++c)
-                hg[c][m] = gam[m][c] - (dvdx[c] * hx + dvdy[c] * hy + dvdz[c] * hz);
+                hg[c][m] = fma(dvdz[c], hz, fma(dvdy[c], hy, fma(dvdx[c], hx, gam[m][c])));
         }
     }
     const double coefficient = -hourg * 0.01 * d.ss[k] * d.elem_mass[k] * r;
