@@ -67,6 +67,39 @@ __device__ __forceinline__ void time_increment(DevScalars *sc, const lulesh_para
 __device__ __forceinline__ double recip(double x) { return __drcp_rn(x); }
 __device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
 
+// Conversions between FP64 and FP32 run on GB300's FP64 pipe at the FP64
+// rate (2 per SM per clock), so this file converts with integer bit
+// operations instead.  Values below FP32's normal range (|v| < 2^-126)
+// become signed zeros; positions, velocities, forces and the element scalars
+// converted here never live there.
+
+// double -> float, mantissa truncated to 23 bits (error < 2^-23 relative).
+__device__ __forceinline__ float d2f(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned hi = (unsigned)(b >> 32);
+    const unsigned sign = hi & 0x80000000u;
+    const int de = (int)((hi >> 20) & 0x7ffu);
+    const unsigned mant = (unsigned)(b >> 29) & 0x7fffffu;
+    if (de == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (mant ? 0x400000u : 0u));   // inf, nan
+    const int fe = de - 1023 + 127;
+    if (fe <= 0) return __uint_as_float(sign);
+    if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned)fe << 23) | mant);
+}
+
+// float -> double, exact (FP32 subnormals become zeros).
+__device__ __forceinline__ double f2d(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned fe = (u >> 23) & 0xffu;
+    const unsigned long long mant = (unsigned long long)(u & 0x7fffffu) << 29;
+    if (fe == 0) return __longlong_as_double((long long)sign);
+    const unsigned long long de = (fe == 0xff) ? 0x7ffULL : (unsigned long long)(fe - 127 + 1023);
+    return __longlong_as_double((long long)(sign | (de << 52) | mant));
+}
+
 // One direction of the monotonic limiter (:2198-2228).
 template <typename T>
 __device__ __forceinline__ T limiter_phi(const T *__restrict__ delv, int i, int bm, int bp,
@@ -119,6 +152,25 @@ __device__ __forceinline__ double sound_term(double pbvc, double e, double vv, d
     return ssc;
 }
 
+// ssc * qlin + qquad with ssc the sound term of the viscosity update.  With
+// kF32Q (split precision, whose Q coefficients qlin/qquad are FP32) the term
+// is formed in FP32: the coefficients carry FP32 precision already, so an
+// FP64 square root would add FP64 work and no accuracy.
+template <bool kF32Q>
+__device__ __forceinline__ double q_term(double pbvc, double e, double vv, double bvc, double p,
+                                         double rho0, bool unit_rho0, double qlin, double qquad)
+{
+    if constexpr (kF32Q) {
+        const float vvf = d2f(vv);
+        float ssc = d2f(pbvc) * d2f(e) + vvf * vvf * d2f(bvc) * d2f(p);
+        if (!unit_rho0) ssc = ssc / d2f(rho0);
+        ssc = (ssc <= .111111e-36f) ? .333333e-18f : sqrtf(ssc);
+        return f2d(ssc * d2f(qlin) + d2f(qquad));
+    } else {
+        return sound_term(pbvc, e, vv, bvc, p, rho0, unit_rho0) * qlin + qquad;
+    }
+}
+
 // The qstop test, ApplyMaterialPropertiesForElems, EvalEOSForElems +
 // CalcEnergyForElems + CalcSoundSpeedForElems and UpdateVolumesForElems for
 // element k (LULESH-OMP.cc:2369-2381, :2384-2782), given its monotonic-Q
@@ -133,6 +185,7 @@ __device__ __forceinline__ double sound_term(double pbvc, double e, double vv, d
 __device__ __forceinline__ void opaque(double &v) { asm volatile("" : "+d"(v)); }
 __device__ __forceinline__ void consume(double v) { asm volatile("" ::"d"(v)); }
 
+template <bool kF32Q = false>
 __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalars *sc, double vnew,
                                                   double qlin, double qquad, int rep = 1)
 {
@@ -190,14 +243,14 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
         if (e_new < emin) e_new = emin;
         const double p_half = eos_pressure(bvc, e_new, comp_half, vnewc, P);
         q_new = 0.;
-        if (!(delvc > 0.)) q_new = sound_term(pbvc, e_new, vhalf, bvc, p_half, rho0, unit_rho0) * qlin + qquad;
+        if (!(delvc > 0.)) q_new = q_term<kF32Q>(pbvc, e_new, vhalf, bvc, p_half, rho0, unit_rho0, qlin, qquad);
         e_new = e_new + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (p_half + q_new));
         if (fabs(e_new) < e_cut) e_new = 0.;
         if (e_new < emin) e_new = emin;
 
         p_new = eos_pressure(bvc, e_new, compression, vnewc, P);
         double q_tilde = 0.;
-        if (!(delvc > 0.)) q_tilde = sound_term(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0) * qlin + qquad;
+        if (!(delvc > 0.)) q_tilde = q_term<kF32Q>(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0, qlin, qquad);
         const double sixth = 1.0 / 6.0;
         e_new = e_new - (7.0 * (p_old + q_old) - 8.0 * (p_half + q_new) + (p_new + q_tilde)) * delvc * sixth;
         if (fabs(e_new) < e_cut) e_new = 0.;

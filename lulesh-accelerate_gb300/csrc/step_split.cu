@@ -5,8 +5,9 @@
 //
 //   FP32  shape-function geometry, stress and Flanagan-Belytschko hourglass
 //         corner forces (IntegrateStressForElems, CalcFBHourglassForceForElems,
-//         LULESH-OMP.cc:853-931, :1233-1558), the characteristic length and
-//         the monotonic-Q gradients and limiter (:1799-1862, :2034-2320);
+//         LULESH-OMP.cc:853-931, :1233-1558), the characteristic length,
+//         the monotonic-Q gradients and limiter (:1799-1862, :2034-2320) and
+//         the sound-speed factor of the viscosity update (:2477-2500);
 //   FP64  node accelerations, velocities and positions (:1613-1683), the
 //         relative volume and its change, the strain rate vdov (:1927-2032),
 //         CalcEnergyForElems / EOS / sound speed / volume update
@@ -31,39 +32,6 @@
 #include <cuda_runtime.h>
 
 namespace lulesh {
-
-// Conversions between FP64 and FP32 run on GB300's FP64 pipe at the FP64
-// rate (2 per SM per clock), so this file converts with integer bit
-// operations instead.  Values below FP32's normal range (|v| < 2^-126)
-// become signed zeros; positions, velocities, forces and the element scalars
-// converted here never live there.
-
-// double -> float, mantissa truncated to 23 bits (error < 2^-23 relative).
-__device__ __forceinline__ float d2f(double v)
-{
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const unsigned hi = (unsigned)(b >> 32);
-    const unsigned sign = hi & 0x80000000u;
-    const int de = (int)((hi >> 20) & 0x7ffu);
-    const unsigned mant = (unsigned)(b >> 29) & 0x7fffffu;
-    if (de == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (mant ? 0x400000u : 0u));   // inf, nan
-    const int fe = de - 1023 + 127;
-    if (fe <= 0) return __uint_as_float(sign);
-    if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
-    return __uint_as_float(sign | ((unsigned)fe << 23) | mant);
-}
-
-// float -> double, exact (FP32 subnormals become zeros).
-__device__ __forceinline__ double f2d(float f)
-{
-    const unsigned u = __float_as_uint(f);
-    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
-    const unsigned fe = (u >> 23) & 0xffu;
-    const unsigned long long mant = (unsigned long long)(u & 0x7fffffu) << 29;
-    if (fe == 0) return __longlong_as_double((long long)sign);
-    const unsigned long long de = (fe == 0xff) ? 0x7ffULL : (unsigned long long)(fe - 127 + 1023);
-    return __longlong_as_double((long long)(sign | (de << 52) | mant));
-}
 
 // v = hi + lo with hi = v truncated to FP32 precision (exact in FP32) and
 // lo = the remainder (exact in FP64, truncated to FP32): hi + lo carries v to
@@ -459,7 +427,7 @@ __device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScal
             d.ql[k] = qlin;
             d.qq[k] = qquad;
         }
-        const double ssn = material_update(d, k, sc, vnew, qlin, qquad, d.reps ? __ldg(d.reps + k) : 1);
+        const double ssn = material_update<true>(d, k, sc, vnew, qlin, qquad, d.reps ? __ldg(d.reps + k) : 1);
         if (kConstraints) constraint_keys(ssn, vdov, d.arealg[k], P, kc, kh);
     }
 }
