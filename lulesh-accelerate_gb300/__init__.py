@@ -144,6 +144,7 @@ _SIGNATURES = {
     "lulesh_run_profiled": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]),
     "lulesh_probe_fp64_peak": (C.c_int, [_dp]),
     "lulesh_probe_pipe_rates": (C.c_int, [_dp]),
+    "lulesh_probe_math": (C.c_int, [_dp]),
     "lulesh_batch_create": (C.c_int, [C.c_int, _ip, _dp, C.c_int, C.c_int, C.POINTER(Parameters),
                                       C.POINTER(C.c_void_p)]),
     "lulesh_batch_destroy": (None, [C.c_void_p]),
@@ -604,6 +605,14 @@ def probe_fp64_peak() -> float:
     t = C.c_double()
     _check(load_library().lulesh_probe_fp64_peak(C.byref(t)))
     return t.value
+
+
+def probe_math() -> dict:
+    """Largest relative differences of the library's inverse cube root and
+    square root from CUDA's rcbrt and sqrt."""
+    e = np.zeros(2)
+    _check(load_library().lulesh_probe_math(_ptr(e)))
+    return {"inv_cbrt_vs_rcbrt": float(e[0]), "x_rsqrt_x_vs_sqrt": float(e[1])}
 
 
 def probe_pipe_rates() -> dict:

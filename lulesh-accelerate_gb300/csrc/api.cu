@@ -827,6 +827,31 @@ int lulesh_probe_fp64_peak(double *tflops)
     return LULESH_OK;
 }
 
+int lulesh_probe_math(double errs[2])
+{
+    if (!errs) return LULESH_ERR_ARG;
+    unsigned long long *keys = nullptr, h[2] = {0, 0};
+    cudaStream_t st = nullptr;
+    const int n = 1 << 20;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&keys, sizeof h) != cudaSuccess) {
+        if (st) cudaStreamDestroy(st);
+        return fail(nullptr, LULESH_ERR_CUDA, "lulesh_probe_math: no usable CUDA device");
+    }
+    cudaError_t e = cudaMemsetAsync(keys, 0, sizeof h, st);
+    if (e == cudaSuccess) {
+        launch_math_probe(keys, n, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, keys, sizeof h, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(keys);
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) return fail(nullptr, LULESH_ERR_CUDA, std::string("lulesh_probe_math: ") + cudaGetErrorString(e));
+    for (int i = 0; i < 2; ++i) std::memcpy(&errs[i], &h[i], sizeof(double));
+    return LULESH_OK;
+}
+
 int lulesh_probe_pipe_rates(double *rates)
 {
     lulesh_ctx *ctx = nullptr;

@@ -100,6 +100,23 @@ __device__ __forceinline__ double f2d(float f)
     return __longlong_as_double((long long)(sign | (de << 52) | mant));
 }
 
+// d^(-1/3) for d > 0 by Newton's iteration on f(y) = y^-3 - d,
+// y <- y + y (1 - d y^3) / 3, from the FP32 estimate rcbrtf: each step
+// squares the relative error (2^-22 -> 2^-44 -> below FP64 rounding), so two
+// steps give the root to a few ulps with ten FP64 operations.
+__device__ __forceinline__ double inv_cbrt(double d)
+{
+    const double third = 1.0 / 3.0;
+    double y = f2d(rcbrtf(d2f(d)));
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const double y3 = (y * y) * y;
+        const double e = fma(-y3, d, 1.0);
+        y = fma(y * e, third, y);
+    }
+    return y;
+}
+
 // One direction of the monotonic limiter (:2198-2228).
 template <typename T>
 __device__ __forceinline__ T limiter_phi(const T *__restrict__ delv, int i, int bm, int bp,

@@ -29,6 +29,9 @@ constexpr int kTimedKernels = 6;   // time increment, force, node, kinematics, m
 void launch_cycle_timed(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTimedKernels + 1]);
 void launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t st);
 void launch_rate_probe(int which, float *out, int blocks, int threads, int iters, cudaStream_t st);
+// largest relative differences (as order keys of non-negative doubles) of the
+// library's inverse cube root and square root from CUDA's, over n arguments
+void launch_math_probe(unsigned long long *keys, int n, cudaStream_t st);
 
 // Split-precision path (step_split.cu).
 void launch_split_sync(const Dom &d, cudaStream_t st);

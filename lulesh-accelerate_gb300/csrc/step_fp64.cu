@@ -104,7 +104,7 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
     // CalcFBHourglassForceForElems (:1291-1473): hourgam = gamma -
     // volinv * (dV/dx . hourmod), with hourmod the gamma projections of the
     // coordinates (modes M6, M5, M4, M7).
-    const double r = rcbrt(determ);                         // determ^(-1/3)
+    const double r = inv_cbrt(determ);                      // determ^(-1/3)
     const double volinv192 = (r * r * r) * (1.0 / 192.0);   // the 1/192 of the derivative
     double hg[8][4];
     {
@@ -487,6 +487,27 @@ void launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStre
 
 // Issue-rate probes for the design notes: 8 independent chains per thread
 // of one operation; each thread writes one value (keeps the chains live).
+// Arguments 2^(120 u - 60) (1 + v) over a grid of u, v; the relative
+// differences of inv_cbrt from rcbrt and of x*rsqrt(x) from sqrt, reduced as
+// the bit patterns of non-negative doubles (which order like the values).
+__global__ void k_math_probe(unsigned long long *keys, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double u = (double)(i >> 10) / 1024.0, v = (double)(i & 1023) / 1024.0;
+    const double x = ldexp(1.0 + v, (int)(120.0 * u) - 60);
+    const double a = rcbrt(x), b = inv_cbrt(x);
+    const double s = sqrt(x), t = x * rsqrt(x);
+    const double ea = fabs(b - a) / a, es = fabs(t - s) / s;
+    atomicMax(keys, (unsigned long long)__double_as_longlong(ea));
+    atomicMax(keys + 1, (unsigned long long)__double_as_longlong(es));
+}
+
+void launch_math_probe(unsigned long long *keys, int n, cudaStream_t st)
+{
+    k_math_probe<<<(n + 255) / 256, 256, 0, st>>>(keys, n);
+}
+
 __global__ void k_probe_ffma(float *out, int iters, float a, float b)
 {
     float r[8];
