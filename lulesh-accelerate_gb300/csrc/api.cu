@@ -355,7 +355,7 @@ int create_from_mesh(const HostMesh &m, int precision, const lulesh_params *para
         A(d.xs, nn); A(d.ys, nn); A(d.zs, nn); A(d.xds, nn); A(d.yds, nn); A(d.zds, nn);
         A(d.gq, 6 * ne);
     }
-    A(d.inv_mass, nn);
+    A(d.inv_mass, nn); A(d.inv_volo, ne);
     A(d.sc, 1); A(ctx->d_active, 1); A(ctx->d_max_cycles, 1);
 #undef A
     d.nodelist = nodelist;
@@ -378,6 +378,8 @@ int create_from_mesh(const HostMesh &m, int precision, const lulesh_params *para
     }
     std::vector<double> zeros(ne, 0.0), ones(ne, 1.0), e(ne, 0.0), inv_mass(nn);
     for (size_t i = 0; i < nn; ++i) inv_mass[i] = 1.0 / m.nodal_mass[i];
+    std::vector<double> inv_volo(ne);
+    for (size_t i = 0; i < ne; ++i) inv_volo[i] = 1.0 / m.volo[i];
     e[m.origin] = m.e0;
     cudaStream_t st = ctx->stream;
     auto up = [&](void *dst, const void *src, size_t bytes) {
@@ -389,7 +391,7 @@ int create_from_mesh(const HostMesh &m, int precision, const lulesh_params *para
               up(letam, m.letam.data(), ne * 4) && up(letap, m.letap.data(), ne * 4) &&
               up(lzetam, m.lzetam.data(), ne * 4) && up(lzetap, m.lzetap.data(), ne * 4) &&
               up(ebc, m.elem_bc.data(), ne * 4) && up(volo, m.volo.data(), ne * 8) &&
-              up(emass, m.elem_mass.data(), ne * 8) && up(nmass, m.nodal_mass.data(), nn * 8) && up(d.inv_mass, inv_mass.data(), nn * 8) &&
+              up(emass, m.elem_mass.data(), ne * 8) && up(nmass, m.nodal_mass.data(), nn * 8) && up(d.inv_mass, inv_mass.data(), nn * 8) && up(d.inv_volo, inv_volo.data(), ne * 8) &&
               up(d.x, m.x.data(), nn * 8) && up(d.y, m.y.data(), nn * 8) && up(d.z, m.z.data(), nn * 8) &&
               up(d.e, e.data(), ne * 8) && up(d.v, ones.data(), ne * 8);
     ok = ok && cudaMemsetAsync(d.xd, 0, nn * 8, st) == cudaSuccess &&

@@ -502,7 +502,7 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
         A(d.xs, nn); A(d.ys, nn); A(d.zs, nn); A(d.xds, nn); A(d.yds, nn); A(d.zds, nn);
         A(d.gq, 6 * ne);
     }
-    A(d.inv_mass, nn);
+    A(d.inv_mass, nn); A(d.inv_volo, ne);
     A(d.sc, (size_t)n); A(b->d_max, 1);
     int *etile_inst_d, *ntile_inst_d, *etile_class_d, *ntile_class_d, *iee, *ine, *eco, *nco;
     A(etile_inst_d, net); A(ntile_inst_d, nnt); A(etile_class_d, net); A(ntile_class_d, nnt);
@@ -569,6 +569,9 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
         std::vector<double> im(nni);
         for (long k2 = 0; k2 < nni; ++k2) im[k2] = 1.0 / m.nodal_mass[k2];
         up(d.inv_mass + no_i, im.data(), nni * 8);
+        std::vector<double> iv(nei);
+        for (long k2 = 0; k2 < nei; ++k2) iv[k2] = 1.0 / m.volo[k2];
+        up(d.inv_volo + eo_i, iv.data(), nei * 8);
         up(d.x + no_i, m.x.data(), nni * 8);
         up(d.y + no_i, m.y.data(), nni * 8);
         up(d.z + no_i, m.z.data(), nni * 8);
@@ -604,7 +607,11 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
         std::vector<double> ones(std::max(ne, nn), 1.0);
         for (int i = 0; i < n; ++i) {
             const long etail = round_tile(b->ne_i[i]) - b->ne_i[i], ntail = round_tile(b->nn_i[i]) - b->nn_i[i];
-            if (etail) { up(volo + b->eoff[i] + b->ne_i[i], ones.data(), etail * 8); up(emass + b->eoff[i] + b->ne_i[i], ones.data(), etail * 8); }
+            if (etail) {
+                up(volo + b->eoff[i] + b->ne_i[i], ones.data(), etail * 8);
+                up(emass + b->eoff[i] + b->ne_i[i], ones.data(), etail * 8);
+                up(d.inv_volo + b->eoff[i] + b->ne_i[i], ones.data(), etail * 8);
+            }
             if (ntail) {
                 up(nmass + b->noff[i] + b->nn_i[i], ones.data(), ntail * 8);
                 up(d.inv_mass + b->noff[i] + b->nn_i[i], ones.data(), ntail * 8);

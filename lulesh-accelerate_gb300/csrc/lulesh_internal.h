@@ -112,6 +112,7 @@ struct Dom {
     float *f32x, *f32y, *f32z;
     float2 *xs, *ys, *zs, *xds, *yds, *zds;
     double *inv_mass;
+    double *inv_volo;                    // [ne] 1/volo (the element kernels need it)
     float *gq;
     DevScalars *sc;
     const int *gate;                     // host-driven run loop: cycle runs while *gate != 0

@@ -243,7 +243,9 @@ __device__ __forceinline__ void elem_kinematics_fp64(const Dom &d, int k, DevSca
     const double volo = d.volo[k];
     const double vol64 = volume64_shared(M1, M2, M3, X);
     const double volume = vol64 * (1.0 / 64.0);
-    const double rel = volume / volo;
+    // volume / volo, as a product with the reciprocal taken at set-up (within
+    // an ulp of the quotient)
+    const double rel = volume * __ldg(d.inv_volo + k);
     d.vnew[k] = rel;
     d.delv[k] = rel - d.v[k];
     // CalcElemCharacteristicLength (:1821-1862): 4V / sqrt(max AreaFace) with

@@ -321,7 +321,9 @@ __device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevSc
         vdov = strain_rate(M1, M2, M3, V3<double>{vx[0], vy[0], vz[0]}, V3<double>{vx[1], vy[1], vz[1]},
                            V3<double>{vx[2], vy[2], vz[2]}, 0.5 * sc->deltatime);
     }
-    const double rel = volume / volo;
+    // volume / volo, as a product with the reciprocal taken at set-up (within
+    // an ulp of the quotient)
+    const double rel = volume * __ldg(d.inv_volo + k);
     d.vnew[k] = rel;
     d.delv[k] = rel - d.v[k];
     d.vdov[k] = vdov;
