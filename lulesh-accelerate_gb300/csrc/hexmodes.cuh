@@ -162,7 +162,7 @@ __device__ __forceinline__ ModeCrosses<T> mode_crosses(const V3<T> &M1, const V3
     return {cross3(M2, M3), cross3(M3, M1), cross3(M1, M2), cross3(M4, M5), cross3(M6, M4), cross3(M5, M6)};
 }
 
-// 64 x volume through the shared crosses: the bilinear terms of volume64 are
+// 64 x volume through the shared crosses: the bilinear terms of the volume formula above are
 // scalar triple products, M4.(M2xM6) = M2.(M6xM4) and M5.(M6xM3) = M3.(M5xM6).
 template <typename T>
 __device__ __forceinline__ T volume64_shared(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
