@@ -36,6 +36,7 @@ PUBLISHED_V1 = {5: (306, 1.670602e+05), 10: (593, 5.174622e+05), 45: (1495, 4.26
                 50: (1566, 4.052502e+05), 70: (1816, 3.453062e+05), 90: (2026, 3.063249e+05)}
 
 RUNS = [  # (s, init, cycle cap or 0)
+    (1, "v1", 0), (2, "v1", 0), (3, "v1", 0), (1, "v2", 0), (2, "v2", 0), (3, "v2", 0),
     (5, "v1", 0), (10, "v1", 0), (45, "v1", 0),
     (4, "v2", 0), (5, "v2", 0), (8, "v2", 0), (10, "v2", 0), (16, "v2", 0), (30, "v2", 0),
     (30, "v2", 100), (48, "v2", 40),

@@ -67,7 +67,8 @@ def test_phase_parity_with_reference(pkg, s, cyc):
         assert sc.dthydro == pytest.approx(st["time_constraints"]["dthydro"], rel=SCALAR_TOL)
 
 
-FULL_RUNS = [(5, "v1", 0), (10, "v1", 0), (45, "v1", 0), (4, "v2", 0), (5, "v2", 0), (8, "v2", 0),
+FULL_RUNS = [(1, "v1", 0), (2, "v1", 0), (3, "v1", 0), (1, "v2", 0), (2, "v2", 0), (3, "v2", 0),
+             (5, "v1", 0), (10, "v1", 0), (45, "v1", 0), (4, "v2", 0), (5, "v2", 0), (8, "v2", 0),
              (10, "v2", 0), (16, "v2", 0), (30, "v2", 0), (30, "v2", 100), (48, "v2", 40)]
 
 

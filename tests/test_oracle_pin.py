@@ -41,7 +41,9 @@ def test_published_table_v1(orc, answers, s):
     assert float(f"{o.field('e')[0]:.6e}") == energy
 
 
-@pytest.mark.parametrize("s,init,cap", [(5, "v1", 0), (10, "v1", 0), (4, "v2", 0), (5, "v2", 0),
+@pytest.mark.parametrize("s,init,cap", [(1, "v1", 0), (2, "v1", 0), (3, "v1", 0), (1, "v2", 0),
+                                        (2, "v2", 0), (3, "v2", 0),
+                                        (5, "v1", 0), (10, "v1", 0), (4, "v2", 0), (5, "v2", 0),
                                         (8, "v2", 0), (10, "v2", 0), (16, "v2", 0), (30, "v2", 100),
                                         (30, "v2", 0)])
 def test_oracle_matches_reference_runs(orc, answers, s, init, cap):
