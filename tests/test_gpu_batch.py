@@ -87,3 +87,19 @@ def test_autotune_restores_state_and_caches(pkg, tmp_path):
     with pkg.Batch(SIZES, SCALE) as c:
         c.autotune(str(cache))                 # served from the cache
         assert c.tuning() == tuned
+
+
+def test_batch_of_tiny_and_single_instances(pkg):
+    """Edge sizes: one-element instances beside larger ones, and a batch of
+    one instance, each equal to its single-instance run."""
+    for sizes, scale in (([1, 2, 3, 1, 7], [1.0, 1.3, 0.8, 0.6, 1.0]), ([5], [1.0])):
+        with pkg.Batch(sizes, scale, pkg.INIT_V2, pkg.FP64) as b:
+            solos = [_solo_like(pkg, b, i, pkg.FP64) for i in range(len(sizes))]
+            b.run()
+            for i, g in enumerate(solos):
+                n = g.run()
+                sc, _, status = b.instance(i)
+                assert status == pkg.OK and sc.cycle == n, (sizes, i)
+                for k in ("x", "e", "p", "v"):
+                    assert np.array_equal(b.get_field(i, k), g.get_field(k)), (sizes, i, k)
+                g.close()
