@@ -63,9 +63,9 @@ def algorithmic_bytes(ne: int, nn: int, precision: str = "fp64") -> dict:
             # slots (32/elem) + start (4/node), FP32 corner forces (96/elem),
             # 1/mass (8) + bc (1), x..zd read and written (96), hi/lo pairs out (48)
             "node_update": (4 + 8 + 1 + 96 + 48) * nn + (32 + 96) * ne,
-            # nodelist, FP64 x..zd and their hi/lo pairs gathered, volo, v in;
-            # vnew delv vdov arealg (FP64) and six FP32 Q gradients out
-            "elem_kinematics": 96 * nn + (32 + 16 + 32 + 24) * ne,
+            # nodelist, hi/lo pairs of x..zd gathered, 1/volo, v in; vnew delv
+            # vdov arealg (FP64) and six FP32 Q gradients out
+            "elem_kinematics": 48 * nn + (32 + 16 + 32 + 24) * ne,
             # bc + neighbour ids, FP32 gradients, vnew vdov delv arealg volo mass
             # q v e p in; p e q ss v out
             "elem_material": (4 + 24 + 24 + 80 + 40) * ne,
@@ -79,8 +79,9 @@ def algorithmic_bytes(ne: int, nn: int, precision: str = "fp64") -> dict:
         # corner slots (32/elem) + start (4/node), corner forces (384/elem),
         # mass (8) + bc (1), x..zd read and written (96)
         "node_update": (4 + 8 + 1 + 96) * nn + (32 + 384) * ne,
-        # nodelist, x..zd gathered, volo, v in; vnew delv arealg vdov delv_* delx_* out
-        "elem_kinematics": 48 * nn + (32 + 16 + 80) * ne,
+        # nodelist, x..zd gathered, volo, 1/volo, v in; vnew delv arealg vdov
+        # delv_* delx_* out
+        "elem_kinematics": 48 * nn + (32 + 24 + 80) * ne,
         # bc + 6 neighbour ids, delv_* delx_*, vnew volo vdov delv mass q v e p
         # arealg in; p e q ss v out
         "elem_material": (4 + 24 + 48 + 80 + 40) * ne,
