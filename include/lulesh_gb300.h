@@ -235,6 +235,25 @@ int lulesh_origin_energy(lulesh_ctx *ctx, double *e0);
 int lulesh_symmetry(lulesh_ctx *ctx, double *max_abs_diff, double *total_abs_diff,
                     double *max_rel_diff);
 
+/* ---- visualisation output --------------------------------------------
+ * The reference writes each step for VisIt with Silo (writeDomain,
+ * cbits/visit.cc:149-177, bound at src/VisIt.hs:71-86): mesh connectivity and
+ * coordinates with the time and cycle, the zone fields e, p, v, q and the
+ * node fields xd, yd, zd and speed.  Silo is not available here, so the same
+ * content goes to a raw structure-of-arrays file ("LULESHD1": a header with
+ * s, elements, nodes, step and time, then named, typed, counted sections;
+ * the layout is spelled out in csrc/output.cpp).  The file name is
+ * printf(basename, step) as in the reference, with at most one %d conversion
+ * allowed.  lulesh_write_domain has the reference's argument list (host
+ * arrays of the s^3 cube, num_elem = s) and needs no GPU;
+ * lulesh_dump_domain writes a context's current state, cube or unstructured.
+ * LULESH_ERR_ARG for a bad pattern, size or file. */
+int lulesh_write_domain(const char *basename, int num_elem, int step, double time,
+                        const double *x, const double *y, const double *z,
+                        const double *xd, const double *yd, const double *zd,
+                        const double *e, const double *p, const double *v, const double *q);
+int lulesh_dump_domain(lulesh_ctx *ctx, const char *basename, int step);
+
 /* Sizes of this context's mesh (s = 0 for an unstructured mesh). */
 int lulesh_sizes(lulesh_ctx *ctx, int *s, long *num_elem, long *num_node);
 

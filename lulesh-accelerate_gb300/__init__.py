@@ -116,6 +116,8 @@ _SIGNATURES = {
                                              C.POINTER(C.c_void_p)]),
     "lulesh_create_lmesh": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(Parameters), C.POINTER(C.c_void_p)]),
     "lulesh_origin_element": (C.c_int, [C.c_void_p, C.POINTER(C.c_long)]),
+    "lulesh_write_domain": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double] + [_dp] * 10),
+    "lulesh_dump_domain": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
     "lulesh_set_regions": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "lulesh_get_regions": (C.c_int, [C.c_void_p, _ip]),
     "lulesh_region_numbers": (C.c_int, [C.c_long, C.c_int, C.c_int, _ip]),
@@ -207,6 +209,36 @@ def default_parameters() -> Parameters:
     p = Parameters()
     load_library().lulesh_default_params(C.byref(p))
     return p
+
+
+def write_domain(basename, s: int, step: int, time: float, fields: dict) -> None:
+    """The reference's per-step visualisation write (cbits/visit.cc
+    writeDomain) for host arrays of the s^3 cube; ``fields`` holds x, y, z,
+    xd, yd, zd, e, p, v, q."""
+    arrs = [np.ascontiguousarray(fields[k], dtype=np.float64)
+            for k in ("x", "y", "z", "xd", "yd", "zd", "e", "p", "v", "q")]
+    _check(load_library().lulesh_write_domain(os.fsencode(str(basename)), s, step, time, *[_ptr(a) for a in arrs]))
+
+
+def read_domain_file(path) -> dict:
+    """A file of ``lulesh_write_domain`` / ``lulesh_dump_domain``: header
+    values (s, num_elem, num_node, step, time) and one array per section."""
+    data = Path(path).read_bytes()
+    if data[:8] != b"LULESHD1":
+        raise ValueError(f"{path}: not a LULESHD1 file")
+    s, ne, nn, step = np.frombuffer(data, np.int32, 4, 8)
+    (time,) = np.frombuffer(data, np.float64, 1, 24)
+    (nsec,) = np.frombuffer(data, np.int32, 1, 32)
+    out = {"s": int(s), "num_elem": int(ne), "num_node": int(nn), "step": int(step), "time": float(time)}
+    off = 36
+    for _ in range(int(nsec)):
+        name = data[off:off + 16].split(b"\0")[0].decode()
+        typ, _centring = np.frombuffer(data, np.int32, 2, off + 16)
+        (count,) = np.frombuffer(data, np.int64, 1, off + 24)
+        dt = np.int32 if typ == 0 else np.float64
+        out[name] = np.frombuffer(data, dt, int(count), off + 32).copy()
+        off += 32 + int(count) * np.dtype(dt).itemsize
+    return out
 
 
 def region_numbers(num_elem: int, num_regions: int, balance: int = 1) -> np.ndarray:
@@ -336,6 +368,11 @@ class Lulesh:
         out = np.empty(self.num_elem, dtype=np.int32)
         _check(load_library().lulesh_get_regions(self._h, _ptr(out, C.c_int)), self._h)
         return out
+
+    def dump(self, basename, step: int) -> None:
+        """Write the current state for visualisation (``read_domain_file``
+        reads it back); ``basename`` may hold one %d for the step."""
+        _check(load_library().lulesh_dump_domain(self._h, os.fsencode(str(basename)), step), self._h)
 
     @property
     def origin(self) -> int:

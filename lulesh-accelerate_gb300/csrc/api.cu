@@ -43,6 +43,12 @@ namespace {
 constexpr int kChunkCycles = 16;     // cycles per graph in the host-driven fallback
 thread_local std::string g_err;
 
+}  // namespace
+
+void lulesh::set_last_error(const std::string &msg) { g_err = msg; }
+
+namespace {
+
 int fail(lulesh_ctx *c, int code, const std::string &msg)
 {
     if (c) c->err = msg;
@@ -469,6 +475,31 @@ int lulesh_create_lmesh(const char *path, int precision, const lulesh_params *pa
     std::string err;
     if (f.read(path, &err) != LULESH_OK) return fail(nullptr, LULESH_ERR_ARG, err);
     return lulesh_create_unstructured(&f.view, precision, params, out);
+}
+
+int lulesh_dump_domain(lulesh_ctx *ctx, const char *basename, int step)
+{
+    if (!ctx) return LULESH_ERR_ARG;
+    const size_t ne = ctx->ne, nn = ctx->nn;
+    std::vector<double> node(6 * nn), elem(4 * ne);
+    std::vector<int> nodelist(8 * ne);
+    const Dom &d = ctx->dom;
+    double *const ndst[6] = {d.x, d.y, d.z, d.xd, d.yd, d.zd};
+    double *const edst[4] = {d.e, d.p, d.v, d.q};
+    for (int i = 0; i < 6; ++i)
+        CK(cudaMemcpyAsync(node.data() + i * nn, ndst[i], nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    for (int i = 0; i < 4; ++i)
+        CK(cudaMemcpyAsync(elem.data() + i * ne, edst[i], ne * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(nodelist.data(), d.nodelist, 8 * ne * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->h_sc, d.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const double *fields[10] = {node.data(), node.data() + nn, node.data() + 2 * nn, node.data() + 3 * nn,
+                                node.data() + 4 * nn, node.data() + 5 * nn, elem.data(), elem.data() + ne,
+                                elem.data() + 2 * ne, elem.data() + 3 * ne};
+    std::string err;
+    const int rc = write_domain_file(basename, ctx->s, (long)ne, (long)nn, nodelist.data(), step, ctx->h_sc->time,
+                                     fields, &err);
+    return rc ? fail(ctx, rc, "lulesh_dump_domain: " + err) : LULESH_OK;
 }
 
 int lulesh_origin_element(lulesh_ctx *ctx, long *elem)

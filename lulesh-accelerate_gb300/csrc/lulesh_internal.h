@@ -79,6 +79,12 @@ double host_elem_volume(const double x[8], const double y[8], const double z[8])
 // of region r (0-based)
 void region_numbers(long ne, int nr, int balance, std::vector<int> &reg);
 int region_reps(int r, int nr, int cost);
+// The visualisation dump (output.cpp): fields in the reference's writeDomain
+// order x y z xd yd zd e p v q; LULESH_OK or LULESH_ERR_ARG with *err set.
+int write_domain_file(const char *basename, int s, long ne, long nn, const int *nodelist, int step,
+                      double time, const double *const fields[10], std::string *err);
+// The message lulesh_last_error(NULL) returns.
+void set_last_error(const std::string &msg);
 void default_params(lulesh_params *p);
 
 // Everything one kernel launch needs, passed by value.

@@ -6,13 +6,23 @@
  * in the reference's format.  It uses only include/lulesh_gb300.h.
  *
  * Usage: lulesh_gb300_main S [--init v1|v2] [--split] [--cycles N] [--calls]
+ *                          [--output PATTERN] [--xyz FILE]
  *        lulesh_gb300_main -u FILE.lmesh [--split] [--cycles N] [--calls]
+ *                          [--output PATTERN] [--xyz FILE]
  *   -u       an unstructured mesh file, as the reference's GPU driver takes it
  *            (reference/CUDA/lulesh-kepler-singlegpu/lulesh.cu:3321-3329);
  *            the plane-0 symmetry test is then skipped, as there
  *   --calls  drive the loop from the host, one lulesh_time_increment +
  *            lulesh_lagrange_leapfrog call per cycle, as the reference's loop
  *            does (default: one lulesh_run call)
+ *   --output write the state before every cycle to PATTERN formatted with the
+ *            cycle number (lulesh_dump_domain), as the Haskell host's
+ *            --output does with writeDomain (src/Main.hs:85-100); implies
+ *            --calls
+ *   --xyz    write the final node positions to FILE in the text layout of
+ *            the reference GPU driver's write_solution
+ *            (reference/CUDA/lulesh-kepler-singlegpu/lulesh.cu:3451-3470):
+ *            per node its index (%10d) and x, y, z (%.10f), one per line
  */
 #include "lulesh_gb300.h"
 
@@ -31,11 +41,14 @@ int main(int argc, char **argv)
     const char *lmesh = !strcmp(argv[1], "-u") ? argv[2] : NULL;
     const int s = lmesh ? 0 : atoi(argv[1]);
     int init = LULESH_INIT_V2, precision = LULESH_PRECISION_FP64, cap = 0, calls = 0;
+    const char *output = NULL, *xyz = NULL;
     for (int i = lmesh ? 3 : 2; i < argc; ++i) {
         if (!strcmp(argv[i], "--init") && i + 1 < argc) init = strcmp(argv[++i], "v1") ? LULESH_INIT_V2 : LULESH_INIT_V1;
         else if (!strcmp(argv[i], "--split")) precision = LULESH_PRECISION_SPLIT;
         else if (!strcmp(argv[i], "--cycles") && i + 1 < argc) cap = atoi(argv[++i]);
         else if (!strcmp(argv[i], "--calls")) calls = 1;
+        else if (!strcmp(argv[i], "--output") && i + 1 < argc) { output = argv[++i]; calls = 1; }
+        else if (!strcmp(argv[i], "--xyz") && i + 1 < argc) xyz = argv[++i];
         else {
             fprintf(stderr, "unknown argument %s\n", argv[i]);
             return 2;
@@ -58,6 +71,7 @@ int main(int argc, char **argv)
         lulesh_scalars sc;
         lulesh_get_scalars(ctx, &sc);
         while (sc.time < prm.stoptime && (cap <= 0 || cycles < cap)) {
+            if (output && (rc = lulesh_dump_domain(ctx, output, cycles))) break;
             if ((rc = lulesh_time_increment(ctx)) || (rc = lulesh_lagrange_leapfrog(ctx))) break;
             lulesh_get_scalars(ctx, &sc);
             ++cycles;
@@ -89,6 +103,24 @@ int main(int argc, char **argv)
         printf("        MaxAbsDiff   = %12.6e\n", ma);
         printf("        TotalAbsDiff = %12.6e\n", ta);
         printf("        MaxRelDiff   = %12.6e\n\n", mr);
+    }
+    if (xyz) {
+        long nn = 0;
+        lulesh_sizes(ctx, NULL, NULL, &nn);
+        double *p = (double *)malloc(3 * (size_t)nn * sizeof(double));
+        FILE *f = p ? fopen(xyz, "w") : NULL;
+        if (!f || lulesh_get_field(ctx, "x", p, nn) || lulesh_get_field(ctx, "y", p + nn, nn) ||
+            lulesh_get_field(ctx, "z", p + 2 * nn, nn)) {
+            fprintf(stderr, "cannot write %s\n", xyz);
+            if (f) fclose(f);
+            free(p);
+            lulesh_destroy(ctx);
+            return 1;
+        }
+        for (long i = 0; i < nn; ++i)
+            fprintf(f, "%10ld\n%.10f\n%.10f\n%.10f\n", i, p[i], p[nn + i], p[2 * nn + i]);
+        fclose(f);
+        free(p);
     }
     printf("{\"cycles\": %d, \"origin_energy\": %.17e, \"max_rel_diff\": %.17e}\n", cycles, e0, mr);
     lulesh_destroy(ctx);
