@@ -63,6 +63,43 @@ __device__ __forceinline__ void time_increment(DevScalars *sc, const lulesh_para
     ++sc->cycle;
 }
 
+// Comparisons of doubles on the integer pipes.  The FP64 unit of this part
+// retires two lanes per SM per clock and an FP64 compare takes one of those
+// slots like an FMA; the integer units are many times wider.  ikey maps a
+// double onto an int64 that orders like the value (sign-magnitude to two's
+// complement; -0 and +0 both map to 0), so for non-NaN operands these give
+// the IEEE results.  The keys are formed in inline PTX so that the compiler
+// keeps them integer work.  The step's error tests (volume, qstop) stay IEEE
+// compares, so that a NaN never raises or hides them differently.
+__device__ __forceinline__ long long ikey(double x)
+{
+    long long k;
+    asm("{\n\t.reg .b64 b, m, s;\n\t"
+        "mov.b64 b, %1;\n\t"
+        "and.b64 m, b, 0x7fffffffffffffff;\n\t"
+        "shr.s64 s, b, 63;\n\t"
+        "xor.b64 m, m, s;\n\t"
+        "sub.s64 %0, m, s;\n\t}"
+        : "=l"(k) : "d"(x));
+    return k;
+}
+// |x| as its bit pattern (orders like |x| for non-NaN x)
+__device__ __forceinline__ unsigned long long iabs(double x)
+{
+    unsigned long long k;
+    asm("{\n\t.reg .b64 b;\n\tmov.b64 b, %1;\n\tand.b64 %0, b, 0x7fffffffffffffff;\n\t}" : "=l"(k) : "d"(x));
+    return k;
+}
+__device__ __forceinline__ bool lt(double a, double b) { return ikey(a) < ikey(b); }
+__device__ __forceinline__ bool le(double a, double b) { return ikey(a) <= ikey(b); }
+__device__ __forceinline__ bool gt(double a, double b) { return ikey(a) > ikey(b); }
+__device__ __forceinline__ bool ge(double a, double b) { return ikey(a) >= ikey(b); }
+// |a| < |c|
+__device__ __forceinline__ bool abs_lt(double a, double c) { return iabs(a) < iabs(c); }
+// FP32 compares are cheap already
+__device__ __forceinline__ bool lt(float a, float b) { return a < b; }
+__device__ __forceinline__ bool gt(float a, float b) { return a > b; }
+
 // 1/x, correctly rounded in both precisions (the bits of a division).
 __device__ __forceinline__ double recip(double x) { return __drcp_rn(x); }
 __device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
@@ -138,10 +175,10 @@ __device__ __forceinline__ T limiter_phi(const T *__restrict__ delv, int i, int 
     T phi = T(.5) * (delvm + delvp);
     delvm *= limiter;
     delvp *= limiter;
-    if (delvm < phi) phi = delvm;
-    if (delvp < phi) phi = delvp;
-    if (phi < T(0.)) phi = T(0.);
-    if (phi > max_slope) phi = max_slope;
+    if (lt(delvm, phi)) phi = delvm;
+    if (lt(delvp, phi)) phi = delvp;
+    if (lt(phi, T(0.))) phi = T(0.);
+    if (gt(phi, max_slope)) phi = max_slope;
     return phi;
 }
 
@@ -152,9 +189,9 @@ __device__ __forceinline__ double eos_pressure(double &bvc, double e, double com
     const double c1s = 2.0 / 3.0;
     bvc = c1s * (comp + 1.);
     double p = bvc * e;
-    if (fabs(p) < P.p_cut) p = 0.0;
-    if (vnewc >= P.eosvmax) p = 0.0;
-    if (p < P.pmin) p = P.pmin;
+    if (abs_lt(p, P.p_cut)) p = 0.0;
+    if (ge(vnewc, P.eosvmax)) p = 0.0;
+    if (lt(p, P.pmin)) p = P.pmin;
     return p;
 }
 
@@ -166,7 +203,7 @@ __device__ __forceinline__ double sound_term(double pbvc, double e, double vv, d
     if (!unit_rho0) ssc = ssc / rho0;   // x / 1.0 == x: the division is skipped only then
     // sqrt(x) as x * rsqrt(x) (x > 1.1e-37 here): within a few ulps of the
     // correctly rounded root at a fraction of its FP64 instructions
-    if (ssc <= .111111e-36) ssc = .333333e-18;
+    if (le(ssc, .111111e-36)) ssc = .333333e-18;
     else ssc = ssc * rsqrt(ssc);
     return ssc;
 }
@@ -217,13 +254,13 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
     // ApplyMaterialPropertiesForElems (:2703-2761)
     const double eosvmin = P.eosvmin, eosvmax = P.eosvmax;
     double vnewc_in = vnew;
-    if (eosvmin != 0. && vnewc_in < eosvmin) vnewc_in = eosvmin;
-    if (eosvmax != 0. && vnewc_in > eosvmax) vnewc_in = eosvmax;
+    if (eosvmin != 0. && lt(vnewc_in, eosvmin)) vnewc_in = eosvmin;
+    if (eosvmax != 0. && gt(vnewc_in, eosvmax)) vnewc_in = eosvmax;
     const double qlin_in = qlin, qquad_in = qquad;
     const double v_old = d.v[k];
     double vc = v_old;
-    if (eosvmin != 0. && vc < eosvmin) vc = eosvmin;
-    if (eosvmax != 0. && vc > eosvmax) vc = eosvmax;
+    if (eosvmin != 0. && lt(vc, eosvmin)) vc = eosvmin;
+    if (eosvmax != 0. && gt(vc, eosvmax)) vc = eosvmax;
     if (vc <= 0.) flag_error(sc, ERR_K3_MATV, k);
 
     // EvalEOSForElems + CalcEnergyForElems (:2415-2701); work == 0
@@ -246,11 +283,11 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
         // vhalf = 1 / (1 + comp_half) (:2460), which is vchalf, vnewc or 1 in the
         // three cases below; taken directly instead of through two divisions
         double vhalf = vchalf;
-        if (eosvmin != 0. && vnewc <= eosvmin) {
+        if (eosvmin != 0. && le(vnewc, eosvmin)) {
             comp_half = compression;
             vhalf = vnewc;
         }
-        if (eosvmax != 0. && vnewc >= eosvmax) {
+        if (eosvmax != 0. && ge(vnewc, eosvmax)) {
             p_old = 0.;
             compression = 0.;
             comp_half = 0.;
@@ -259,28 +296,28 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
         const double emin = P.emin, e_cut = P.e_cut;
 
         e_new = e_old - .5 * delvc * (p_old + q_old);
-        if (e_new < emin) e_new = emin;
+        if (lt(e_new, emin)) e_new = emin;
         const double p_half = eos_pressure(bvc, e_new, comp_half, vnewc, P);
         q_new = 0.;
-        if (!(delvc > 0.)) q_new = q_term<kF32Q>(pbvc, e_new, vhalf, bvc, p_half, rho0, unit_rho0, qlin, qquad);
+        if (!gt(delvc, 0.)) q_new = q_term<kF32Q>(pbvc, e_new, vhalf, bvc, p_half, rho0, unit_rho0, qlin, qquad);
         e_new = e_new + .5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (p_half + q_new));
-        if (fabs(e_new) < e_cut) e_new = 0.;
-        if (e_new < emin) e_new = emin;
+        if (abs_lt(e_new, e_cut)) e_new = 0.;
+        if (lt(e_new, emin)) e_new = emin;
 
         p_new = eos_pressure(bvc, e_new, compression, vnewc, P);
         double q_tilde = 0.;
-        if (!(delvc > 0.)) q_tilde = q_term<kF32Q>(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0, qlin, qquad);
+        if (!gt(delvc, 0.)) q_tilde = q_term<kF32Q>(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0, qlin, qquad);
         const double sixth = 1.0 / 6.0;
         e_new = e_new - (7.0 * (p_old + q_old) - 8.0 * (p_half + q_new) + (p_new + q_tilde)) * delvc * sixth;
-        if (fabs(e_new) < e_cut) e_new = 0.;
-        if (e_new < emin) e_new = emin;
+        if (abs_lt(e_new, e_cut)) e_new = 0.;
+        if (lt(e_new, emin)) e_new = emin;
 
         p_new = eos_pressure(bvc, e_new, compression, vnewc, P);
         // CalcSoundSpeedForElems (:2543-2561) takes the last evaluation's
         ssn = sound_term(pbvc, e_new, vnewc, bvc, p_new, rho0, unit_rho0);
-        if (delvc <= 0.) {
+        if (le(delvc, 0.)) {
             q_new = ssn * qlin + qquad;
-            if (fabs(q_new) < P.q_cut) q_new = 0.;
+            if (abs_lt(q_new, P.q_cut)) q_new = 0.;
         }
         if (rep > 1) {
             consume(p_new); consume(e_new); consume(q_new); consume(ssn);
@@ -293,7 +330,7 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
 
     // UpdateVolumesForElems (:2763-2782)
     double vt = vnew;
-    if (fabs(vt - 1.0) < P.v_cut) vt = 1.0;
+    if (abs_lt(vt - 1.0, P.v_cut)) vt = 1.0;
     d.v[k] = vt;
     return ssn;
 }
@@ -302,8 +339,8 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
 // it never wins a minimum, as in the reference's '<' tests).
 __device__ __forceinline__ unsigned long long order_key(double v)
 {
-    if (v != v) return ~0ULL;
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    if (iabs(v) > 0x7ff0000000000000ULL) return ~0ULL;   // NaN
     return (b & 0x8000000000000000ULL) ? ~b : (b | 0x8000000000000000ULL);
 }
 __device__ __forceinline__ double key_value(unsigned long long k)
@@ -352,10 +389,10 @@ __device__ __forceinline__ void constraint_keys(double ss, double vdov, double a
 {
     kc = ~0ULL;
     kh = ~0ULL;
-    if (vdov != 0.) {
+    if (iabs(vdov) != 0ULL) {
         const double qqc2 = 64.0 * P.qqc * P.qqc;
         double dtf = ss * ss;
-        if (vdov < 0.) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
+        if (lt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
         dtf = arealg * rsqrt(dtf);      // arealg / sqrt(dtf)
         kc = order_key(dtf);
         kh = order_key(P.dvovmax / (fabs(vdov) + 1.e-20));

@@ -196,9 +196,9 @@ __device__ __forceinline__ void node_update_fp64(const Dom &d, int n, const DevS
         az = (bc & 4) ? 0.0 : fz / m;
     }
     double t;
-    t = d.xd[n] + ax * dt; if (fabs(t) < u_cut) t = 0.0; d.xd[n] = t; d.x[n] += t * dt;
-    t = d.yd[n] + ay * dt; if (fabs(t) < u_cut) t = 0.0; d.yd[n] = t; d.y[n] += t * dt;
-    t = d.zd[n] + az * dt; if (fabs(t) < u_cut) t = 0.0; d.zd[n] = t; d.z[n] += t * dt;
+    t = d.xd[n] + ax * dt; if (abs_lt(t, u_cut)) t = 0.0; d.xd[n] = t; d.x[n] += t * dt;
+    t = d.yd[n] + ay * dt; if (abs_lt(t, u_cut)) t = 0.0; d.yd[n] = t; d.y[n] += t * dt;
+    t = d.zd[n] + az * dt; if (abs_lt(t, u_cut)) t = 0.0; d.zd[n] = t; d.z[n] += t * dt;
 }
 
 __global__ void __launch_bounds__(kBlockNode) k_node_update(const __grid_constant__ Dom d)
@@ -309,16 +309,16 @@ __device__ __forceinline__ void elem_material_fp64(const Dom &d, int k, DevScala
                                            lim, maxs);
         const double vnew = d.vnew[k], volo = d.volo[k], vdov = d.vdov[k];
         double qlin, qquad;
-        if (vdov > 0.) {
+        if (gt(vdov, 0.)) {
             qlin = 0.;
             qquad = 0.;
         } else {
             double dxi = d.delv_xi[k] * d.delx_xi[k];
             double deta = d.delv_eta[k] * d.delx_eta[k];
             double dzeta = d.delv_zeta[k] * d.delx_zeta[k];
-            if (dxi > 0.) dxi = 0.;
-            if (deta > 0.) deta = 0.;
-            if (dzeta > 0.) dzeta = 0.;
+            if (gt(dxi, 0.)) dxi = 0.;
+            if (gt(deta, 0.)) deta = 0.;
+            if (gt(dzeta, 0.)) dzeta = 0.;
             const double rho = d.elem_mass[k] / (volo * vnew);
             qlin = -P.qlc_monoq * rho *
                    ((dxi * (1. - phixi) + deta * (1. - phieta)) + dzeta * (1. - phizeta));

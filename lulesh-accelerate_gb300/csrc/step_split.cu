@@ -270,11 +270,11 @@ __device__ __forceinline__ void node_update_split(const Dom &d, int n, const Dev
     const double ay = (bc & 2) ? 0.0 : fy * im;
     const double az = (bc & 4) ? 0.0 : fz * im;
     double t, p;
-    t = d.xd[n] + ax * dt; if (fabs(t) < u_cut) t = 0.0; p = d.x[n] + t * dt;
+    t = d.xd[n] + ax * dt; if (abs_lt(t, u_cut)) t = 0.0; p = d.x[n] + t * dt;
     d.xd[n] = t; d.x[n] = p; d.xds[n] = split_hi_lo(t); d.xs[n] = split_hi_lo(p);
-    t = d.yd[n] + ay * dt; if (fabs(t) < u_cut) t = 0.0; p = d.y[n] + t * dt;
+    t = d.yd[n] + ay * dt; if (abs_lt(t, u_cut)) t = 0.0; p = d.y[n] + t * dt;
     d.yd[n] = t; d.y[n] = p; d.yds[n] = split_hi_lo(t); d.ys[n] = split_hi_lo(p);
-    t = d.zd[n] + az * dt; if (fabs(t) < u_cut) t = 0.0; p = d.z[n] + t * dt;
+    t = d.zd[n] + az * dt; if (abs_lt(t, u_cut)) t = 0.0; p = d.z[n] + t * dt;
     d.zd[n] = t; d.z[n] = p; d.zds[n] = split_hi_lo(t); d.zs[n] = split_hi_lo(p);
 }
 
@@ -411,7 +411,7 @@ __device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScal
                                                  lim, maxs);
         const double vnew = d.vnew[k], vdov = d.vdov[k];
         double qlin = 0., qquad = 0.;
-        if (!(vdov > 0.)) {
+        if (!gt(vdov, 0.)) {
             float dxi = dv_xi[k] * d.gq[3 * ne + k];
             float deta = dv_eta[k] * d.gq[4 * ne + k];
             float dzeta = dv_zeta[k] * d.gq[5 * ne + k];
