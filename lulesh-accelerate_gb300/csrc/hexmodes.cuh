@@ -193,7 +193,18 @@ __device__ __forceinline__ T max_face_cross2_64(const V3<T> &M1, const V3<T> &M2
     const T f1 = pair(C.c23, C.c45, b, a, T(-1.0));   // Y1 = b - a
     const T f2 = pair(C.c31, C.c64, c, a, T(1.0));    // Y2 = c + a
     const T f3 = pair(C.c12, C.c56, c, b, T(1.0));    // |Y3| = |c + b|
-    return fmax(fmax(f1, f2), f3);
+    if constexpr (sizeof(T) == 8) {
+        // the three are >= 0, so their bit patterns order like the values:
+        // compare those on the integer pipes instead of two FP64 max slots
+        unsigned long long k1, k2, k3;
+        asm("mov.b64 %0, %1;" : "=l"(k1) : "d"(f1));
+        asm("mov.b64 %0, %1;" : "=l"(k2) : "d"(f2));
+        asm("mov.b64 %0, %1;" : "=l"(k3) : "d"(f3));
+        const T m12 = k1 > k2 ? f1 : f2;
+        return (k1 > k2 ? k1 : k2) > k3 ? m12 : f3;
+    } else {
+        return fmax(fmax(f1, f2), f3);
+    }
 }
 
 // The strain rate tr(grad v) at the half step (CalcElemVelocityGrandient +
