@@ -12,8 +12,8 @@
 //
 // Execution.  One cycle is: a per-instance TimeIncrement; the four step
 // kernels, each a persistent kernel per size class walking that class's list
-// of active tiles (the classes run as parallel graph branches); a
-// per-instance epilogue that publishes the constraint minima, counts the
+// of active tiles (each class's chain of four is one parallel graph branch);
+// a per-instance epilogue that publishes the constraint minima, counts the
 // cycle and retires instances that reached their stop time; and a compaction
 // of the active-tile lists when an instance retired.  The whole run is one
 // CUDA graph with a conditional WHILE node that loops while any instance is
@@ -213,30 +213,33 @@ unsigned compact_blocks(const lulesh_batch *b)
     return (unsigned)((t + 255) / 256);
 }
 
-// One cycle on b->stream; the size classes of each kernel run as parallel
-// branches (fork/join through events, which stream capture turns into graph
-// edges).
+// One cycle on b->stream; each size class runs its four kernels as one
+// parallel branch (fork/join through events, which stream capture turns into
+// graph edges).
 void launch_cycle(lulesh_batch *b, cudaGraphConditionalHandle h)
 {
     cudaStream_t st = b->stream;
     kb_time_increment<<<(b->n + 127) / 128, 128, 0, st>>>(b->dom, b->bv);
-    for (int k = 0; k < kBatchKernels; ++k) {
-        int first = -1;
-        for (int c = 0; c < kMaxClasses; ++c)
-            if ((k == 1 ? b->class_ntiles[c] : b->class_etiles[c]) > 0) {
-                if (first < 0) first = c;
-            }
-        cudaEventRecord(b->ev_fork, st);
-        for (int c = 0; c < kMaxClasses; ++c) {
-            if ((k == 1 ? b->class_ntiles[c] : b->class_etiles[c]) == 0) continue;
-            if (c == first) {
-                launch_kernel(b, k, c, st);
-            } else {
-                cudaStreamWaitEvent(b->side[c], b->ev_fork, 0);
-                launch_kernel(b, k, c, b->side[c]);
-                cudaEventRecord(b->ev_join[c], b->side[c]);
-                cudaStreamWaitEvent(st, b->ev_join[c], 0);
-            }
+    // Instances never interact, so each size class runs its whole chain of
+    // four phases on its own branch: a class that finishes a phase goes on
+    // to its next one while the others are still busy, instead of waiting
+    // at a join after every phase.  The branches join before the epilogue.
+    int first = -1;
+    for (int c = 0; c < kMaxClasses; ++c)
+        if (b->class_etiles[c] > 0 || b->class_ntiles[c] > 0) {
+            first = c;
+            break;
+        }
+    cudaEventRecord(b->ev_fork, st);
+    for (int c = 0; c < kMaxClasses; ++c) {
+        if (b->class_etiles[c] == 0 && b->class_ntiles[c] == 0) continue;
+        cudaStream_t sc = c == first ? st : b->side[c];
+        if (c != first) cudaStreamWaitEvent(sc, b->ev_fork, 0);
+        for (int k = 0; k < kBatchKernels; ++k)
+            if ((k == 1 ? b->class_ntiles[c] : b->class_etiles[c]) > 0) launch_kernel(b, k, c, sc);
+        if (c != first) {
+            cudaEventRecord(b->ev_join[c], sc);
+            cudaStreamWaitEvent(st, b->ev_join[c], 0);
         }
     }
     kb_epilogue<<<1, 1024, 0, st>>>(b->dom, b->bv, h);
