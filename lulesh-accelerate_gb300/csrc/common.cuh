@@ -90,6 +90,15 @@ __device__ __forceinline__ unsigned long long iabs(double x)
     asm("{\n\t.reg .b64 b;\n\tmov.b64 b, %1;\n\tand.b64 %0, b, 0x7fffffffffffffff;\n\t}" : "=l"(k) : "d"(x));
     return k;
 }
+// -x by flipping the sign bit on the integer pipes (a negation the compiler
+// cannot fold into a neighbouring operation otherwise costs an FP64 add)
+__device__ __forceinline__ double neg(double x)
+{
+    double r;
+    asm("{\n\t.reg .b64 b;\n\tmov.b64 b, %1;\n\txor.b64 b, b, 0x8000000000000000;\n\tmov.b64 %0, b;\n\t}"
+        : "=d"(r) : "d"(x));
+    return r;
+}
 __device__ __forceinline__ bool lt(double a, double b) { return ikey(a) < ikey(b); }
 __device__ __forceinline__ bool le(double a, double b) { return ikey(a) <= ikey(b); }
 __device__ __forceinline__ bool gt(double a, double b) { return ikey(a) > ikey(b); }

@@ -77,9 +77,9 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
             d.fsx[c * ne + k] = fx;
             d.fsy[c * ne + k] = fy;
             d.fsz[c * ne + k] = fz;
-            d.fsx[neg_of[c] * ne + k] = -fx;
-            d.fsy[neg_of[c] * ne + k] = -fy;
-            d.fsz[neg_of[c] * ne + k] = -fz;
+            d.fsx[neg_of[c] * ne + k] = neg(fx);
+            d.fsy[neg_of[c] * ne + k] = neg(fy);
+            d.fsz[neg_of[c] * ne + k] = neg(fz);
         }
         const double determ64 = dot3(M2, cross3(M3, M1));
         if (determ64 <= 0.0) flag_error(sc, ERR_K1_DETERM, k);
