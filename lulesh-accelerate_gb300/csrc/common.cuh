@@ -263,19 +263,21 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
     // ApplyMaterialPropertiesForElems (:2703-2761)
     const double eosvmin = P.eosvmin, eosvmax = P.eosvmax;
     double vnewc_in = vnew;
-    if (eosvmin != 0. && lt(vnewc_in, eosvmin)) vnewc_in = eosvmin;
-    if (eosvmax != 0. && gt(vnewc_in, eosvmax)) vnewc_in = eosvmax;
+    // eosvmin/eosvmax != 0 (a zero bound switches the bound off)
+    const bool has_vmin = iabs(eosvmin) != 0ULL, has_vmax = iabs(eosvmax) != 0ULL;
+    if (has_vmin && lt(vnewc_in, eosvmin)) vnewc_in = eosvmin;
+    if (has_vmax && gt(vnewc_in, eosvmax)) vnewc_in = eosvmax;
     const double qlin_in = qlin, qquad_in = qquad;
     const double v_old = d.v[k];
     double vc = v_old;
-    if (eosvmin != 0. && lt(vc, eosvmin)) vc = eosvmin;
-    if (eosvmax != 0. && gt(vc, eosvmax)) vc = eosvmax;
+    if (has_vmin && lt(vc, eosvmin)) vc = eosvmin;
+    if (has_vmax && gt(vc, eosvmax)) vc = eosvmax;
     if (vc <= 0.) flag_error(sc, ERR_K3_MATV, k);
 
     // EvalEOSForElems + CalcEnergyForElems (:2415-2701); work == 0
     const double delvc_in = d.delv[k], e_old_in = d.e[k], p_old_in = d.p[k];
     const double rho0 = P.refdens;
-    const bool unit_rho0 = (rho0 == 1.0);
+    const bool unit_rho0 = ikey(rho0) == ikey(1.0);
     const double pbvc = 2.0 / 3.0;
     double p_new, e_new, q_new, bvc, ssn;
     for (int j = 0; j < rep; ++j) {
@@ -292,11 +294,11 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
         // vhalf = 1 / (1 + comp_half) (:2460), which is vchalf, vnewc or 1 in the
         // three cases below; taken directly instead of through two divisions
         double vhalf = vchalf;
-        if (eosvmin != 0. && le(vnewc, eosvmin)) {
+        if (has_vmin && le(vnewc, eosvmin)) {
             comp_half = compression;
             vhalf = vnewc;
         }
-        if (eosvmax != 0. && ge(vnewc, eosvmax)) {
+        if (has_vmax && ge(vnewc, eosvmax)) {
             p_old = 0.;
             compression = 0.;
             comp_half = 0.;

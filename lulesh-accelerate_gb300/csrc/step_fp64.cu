@@ -91,7 +91,7 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
     if (vk <= 0.0) flag_error(sc, ERR_K1_VOLUME, k);
 
     const double hourg = d.prm.hgcoef;
-    if (!(hourg > 0.0)) {
+    if (!gt(hourg, 0.0)) {
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
             d.fhx[c * ne + k] = 0.0;
@@ -164,8 +164,20 @@ __device__ __forceinline__ void node_update_fp64(const Dom &d, int n, const DevS
 {
 
     const int st = __ldg(d.corner_start + n), en = __ldg(d.corner_start + n + 1);
+    // the sums start from the first corner rather than from 0.0 (the same
+    // value: x + 0.0 == x, up to the sign of a zero sum), one FP64 add fewer
+    // per component; every node belongs to at least one element
     double sx = 0.0, sy = 0.0, sz = 0.0, hx = 0.0, hy = 0.0, hz = 0.0;
-    for (int i = st; i < en; ++i) {
+    if (st < en) {
+        const int c = __ldg(d.corner_list + st);
+        sx = d.fsx[c];
+        sy = d.fsy[c];
+        sz = d.fsz[c];
+        hx = d.fhx[c];
+        hy = d.fhy[c];
+        hz = d.fhz[c];
+    }
+    for (int i = st + 1; i < en; ++i) {
         const int c = __ldg(d.corner_list + i);
         sx += d.fsx[c];
         sy += d.fsy[c];
