@@ -83,3 +83,27 @@ def test_split_deterministic_and_step_calls_equal_run(pkg):
             b.lagrange_leapfrog()
         for k in ("x", "xd", "e", "p", "q", "v", "ss"):
             assert np.array_equal(a.get_field(k), b.get_field(k)), k
+
+
+def test_split_checkpoint_restart_bitwise(pkg):
+    """Split precision keeps no state beyond the FP64 Domain: k cycles ->
+    download -> upload into a fresh split context (which rebuilds its hi/lo
+    pairs) -> continue == the uninterrupted split run, bit for bit."""
+    s, k, n = 10, 40, 90
+    with pkg.Lulesh(s, pkg.INIT_V2, pkg.SPLIT) as full:
+        full.run(n)
+        want = full.download()
+        want_sc = full.scalars
+    with pkg.Lulesh(s, pkg.INIT_V2, pkg.SPLIT) as a:
+        a.run(k)
+        dom = a.download()
+        sc = a.scalars
+    with pkg.Lulesh(s, pkg.INIT_V2, pkg.SPLIT) as b:
+        b.upload(dom)
+        b.scalars = sc
+        b.run(n - k)
+        got = b.download()
+        got_sc = b.scalars
+    for x, y in zip(got.arrays(), want.arrays()):
+        assert np.array_equal(x, y)
+    assert got_sc.cycle == want_sc.cycle and got_sc.time == want_sc.time

@@ -121,3 +121,25 @@ def test_c_driver_unstructured(pkg, lmesh_dir, mode):
     assert res["cycles"] == ref["cycles"]
     assert abs(res["origin_energy"] - ref["origin_energy"]) <= E0_TOL * ref["origin_energy"]
     assert "Problem size        =  875" in r.stdout
+
+
+def test_regions_on_unstructured_mesh(pkg, lmesh_dir):
+    """LULESH 2.0 regions apply to any element numbering: results bitwise
+    unchanged on the reference's unstructured mesh, in both precisions."""
+    for prec in (pkg.FP64, pkg.SPLIT):
+        with pkg.Lulesh.from_lmesh(lmesh_dir / "sedov15oct.lmesh", precision=prec) as a, \
+                pkg.Lulesh.from_lmesh(lmesh_dir / "sedov15oct.lmesh", precision=prec) as b:
+            b.set_regions(11, 1, 1)
+            assert a.run(100) == 100 and b.run(100) == 100
+            for k in ("x", "y", "z", "xd", "e", "p", "q", "v", "ss"):
+                np.testing.assert_array_equal(a.get_field(k), b.get_field(k), err_msg=k)
+
+
+def test_split_run_sedov21oct_against_reference(pkg, lmesh_dir):
+    """Split precision on the larger reference mesh: same cycle count and
+    origin energy within the split tolerance."""
+    ref = UNSTRUCTURED["meshes"]["sedov21oct"]
+    with pkg.Lulesh.from_lmesh(lmesh_dir / "sedov21oct.lmesh", precision=pkg.SPLIT) as g:
+        assert g.run() == ref["cycles"]
+        e0 = g.origin_energy()
+        assert abs(e0 - ref["origin_energy"]) <= SPLIT_E0_TOL * ref["origin_energy"], (e0, ref["origin_energy"])
