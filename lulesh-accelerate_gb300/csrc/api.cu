@@ -338,6 +338,12 @@ int create_from_mesh(const HostMesh &m, int precision, const lulesh_params *para
     d.keep = 0;
     if (params) d.prm = *params;
     else default_params(&d.prm);
+    {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess || sms < 1)
+            sms = 1;
+        choose_blocks(d, sms);
+    }
     const size_t ne = m.ne, nn = m.nn;
 
     int *nodelist, *cstart, *clist, *lxim, *lxip, *letam, *letap, *lzetam, *lzetap, *ebc;

@@ -13,6 +13,21 @@ namespace lulesh {
 constexpr int kBlockElem = 128;
 constexpr int kBlockNode = 256;
 
+inline int elem_block(const Dom &d) { return d.eblock ? d.eblock : kBlockElem; }
+inline int node_block(const Dom &d) { return d.nblock ? d.nblock : kBlockNode; }
+// Block sizes for a mesh of ne elements and nn nodes on a GPU with sms SMs:
+// the defaults, halved (down to one warp) while a kernel would have fewer
+// than four blocks per SM -- one FP64-bound element per thread makes the SM
+// with one block more than its neighbours the one that sets the time.
+inline void choose_blocks(Dom &d, int sms)
+{
+    int eb = kBlockElem, nb = kBlockNode;
+    while (eb > 32 && (d.ne + eb - 1) / eb < 4L * sms) eb /= 2;
+    while (nb > 32 && (d.nn + nb - 1) / nb < 4L * sms) nb /= 2;
+    d.eblock = eb;
+    d.nblock = nb;
+}
+
 // Plain FP64 path (step_fp64.cu).
 void launch_time_increment(const Dom &d, cudaStream_t st);
 void launch_lagrange_nodal(const Dom &d, cudaStream_t st);

@@ -100,6 +100,10 @@ struct Dom {
     // LULESH 2.0 regions (null without): the material kernel visits elements
     // in mat_order (grouped by cost) and evaluates the EOS reps[k] times
     const int *mat_order, *reps;
+    // threads per block of the element and node kernels (0: kBlockElem /
+    // kBlockNode); smaller on small meshes so that the blocks spread over
+    // every SM
+    int eblock, nblock;
     const double *volo, *elem_mass, *nodal_mass;
     // nodal state
     double *x, *y, *z, *xd, *yd, *zd;

@@ -411,22 +411,22 @@ void launch_time_increment(const Dom &d, cudaStream_t st)
 
 void launch_lagrange_nodal(const Dom &d, cudaStream_t st)
 {
-    k_elem_force<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
-    k_node_update<<<blocks_for(d.nn, kBlockNode), kBlockNode, 0, st>>>(d);
+    k_elem_force<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    k_node_update<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
 }
 
 void launch_lagrange_elements(const Dom &d, cudaStream_t st, bool with_constraints)
 {
-    k_elem_kinematics<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    k_elem_kinematics<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     if (with_constraints)
-        k_elem_material<true><<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+        k_elem_material<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     else
-        k_elem_material<false><<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+        k_elem_material<false><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
 }
 
 void launch_time_constraints(const Dom &d, cudaStream_t st)
 {
-    k_time_constraints<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    k_time_constraints<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     k_finalize<<<1, 1, 0, st>>>(d);
 }
 
@@ -466,13 +466,13 @@ void launch_cycle_timed(const Dom &d, cudaStream_t st, cudaEvent_t ev[7])
     cudaEventRecord(ev[0], st);
     k_time_increment<<<1, 1, 0, st>>>(d);
     cudaEventRecord(ev[1], st);
-    k_elem_force<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    k_elem_force<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     cudaEventRecord(ev[2], st);
-    k_node_update<<<blocks_for(d.nn, kBlockNode), kBlockNode, 0, st>>>(d);
+    k_node_update<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
     cudaEventRecord(ev[3], st);
-    k_elem_kinematics<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    k_elem_kinematics<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     cudaEventRecord(ev[4], st);
-    k_elem_material<true><<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    k_elem_material<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     cudaEventRecord(ev[5], st);
     k_finalize<<<1, 1, 0, st>>>(d);
     cudaEventRecord(ev[6], st);

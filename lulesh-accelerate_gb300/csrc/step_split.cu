@@ -453,22 +453,22 @@ static inline unsigned blocks_for(long n, int bs) { return (unsigned)((n + bs - 
 
 void launch_split_sync(const Dom &d, cudaStream_t st)
 {
-    k_split_sync<<<blocks_for(d.nn, kBlockNode), kBlockNode, 0, st>>>(d);
+    k_split_sync<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
 }
 
 void launch_lagrange_nodal_split(const Dom &d, cudaStream_t st)
 {
-    k_elem_force_split<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
-    k_node_update_split<<<blocks_for(d.nn, kBlockNode), kBlockNode, 0, st>>>(d);
+    k_elem_force_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    k_node_update_split<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
 }
 
 void launch_lagrange_elements_split(const Dom &d, cudaStream_t st, bool with_constraints)
 {
-    k_elem_kinematics_split<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    k_elem_kinematics_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     if (with_constraints)
-        k_elem_material_split<true><<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+        k_elem_material_split<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     else
-        k_elem_material_split<false><<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+        k_elem_material_split<false><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
 }
 
 void launch_run_body_split(const Dom &d, cudaStream_t st, cudaGraphConditionalHandle h, int *active)
@@ -484,13 +484,13 @@ void launch_cycle_timed_split(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTim
     cudaEventRecord(ev[0], st);
     launch_time_increment(d, st);
     cudaEventRecord(ev[1], st);
-    k_elem_force_split<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    k_elem_force_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     cudaEventRecord(ev[2], st);
-    k_node_update_split<<<blocks_for(d.nn, kBlockNode), kBlockNode, 0, st>>>(d);
+    k_node_update_split<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
     cudaEventRecord(ev[3], st);
-    k_elem_kinematics_split<<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    k_elem_kinematics_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     cudaEventRecord(ev[4], st);
-    k_elem_material_split<true><<<blocks_for(d.ne, kBlockElem), kBlockElem, 0, st>>>(d);
+    k_elem_material_split<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     cudaEventRecord(ev[5], st);
     launch_finalize(d, st);
     cudaEventRecord(ev[6], st);
