@@ -74,11 +74,11 @@ def algorithmic_bytes(ne: int, nn: int, precision: str = "fp64") -> dict:
     return {
         "time_increment": 0,
         # x,y,z,xd,yd,zd gathered (48/node), nodelist (32), p q v volo ss mass
-        # (48) in; stress + hourglass corner forces (2 x 24 doubles) out
-        "elem_force": 48 * nn + (32 + 48 + 384) * ne,
-        # corner slots (32/elem) + start (4/node), corner forces (384/elem),
-        # mass (8) + bc (1), x..zd read and written (96)
-        "node_update": (4 + 8 + 1 + 96) * nn + (32 + 384) * ne,
+        # (48) in; corner forces (24 doubles, stress plus hourglass) out
+        "elem_force": 48 * nn + (32 + 48 + 192) * ne,
+        # corner slots (32/elem) + start (4/node), corner forces (192/elem),
+        # 1/mass (8) + bc (1), x..zd read and written (96)
+        "node_update": (4 + 8 + 1 + 96) * nn + (32 + 192) * ne,
         # nodelist, x..zd gathered, volo, 1/volo, v in; vnew delv arealg vdov
         # delv_* delx_* out
         "elem_kinematics": 48 * nn + (32 + 24 + 80) * ne,

@@ -311,7 +311,7 @@ int lulesh_probe_math(double errs[2]);
  *
  * Its working memory (per-corner forces, node-to-corner slots, the
  * symmetry-plane mask, error words) is one fixed device array compiled into
- * the library: at most 65,536 elements and 131,072 nodes, 26.6 MiB that every
+ * the library: at most 65,536 elements and 131,072 nodes, 14.6 MiB that every
  * GPU on which this call is used keeps until the process exits.  All calls
  * share that array, so calls that overlap on the GPU race; order them on one
  * stream.  The first call on a device looks up the array's address with that

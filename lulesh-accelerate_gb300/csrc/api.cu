@@ -360,8 +360,7 @@ int create_from_mesh(const HostMesh &m, int precision, const lulesh_params *para
     A(d.delv_xi, ne); A(d.delv_eta, ne); A(d.delv_zeta, ne);
     A(d.delx_xi, ne); A(d.delx_eta, ne); A(d.delx_zeta, ne);
     if (precision == LULESH_PRECISION_FP64) {
-        A(d.fsx, 8 * ne); A(d.fsy, 8 * ne); A(d.fsz, 8 * ne);
-        A(d.fhx, 8 * ne); A(d.fhy, 8 * ne); A(d.fhz, 8 * ne);
+        A(d.fcx, 8 * ne); A(d.fcy, 8 * ne); A(d.fcz, 8 * ne);
     } else {
         A(d.f32x, 8 * ne); A(d.f32y, 8 * ne); A(d.f32z, 8 * ne);
         A(d.xs, nn); A(d.ys, nn); A(d.zs, nn); A(d.xds, nn); A(d.yds, nn); A(d.zds, nn);

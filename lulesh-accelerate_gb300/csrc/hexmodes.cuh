@@ -107,19 +107,19 @@ __device__ __forceinline__ void inv_walsh6(T q1, T q2, T q3, T q4, T q5, T q6, T
 }
 
 // 192 x the volume derivative of each corner (dx/dy/dz[c] = 192 dV/dx_c)
-// and 64 x the node normals of corners 0..3 (the normals of corners 4..7 are
-// those of 2, 3, 0, 1 negated).  The node normals, sums of the quarter-area
-// vectors of each corner's three faces (CalcElemNodeNormals :708-799), are
-// linear in the corner's signs: pf[c] = (s_xi X1 + s_eta X2 + s_zeta X3)/64
-// with X1 = M2xM3 + M4xM5, X2 = M3xM1 + M6xM4, X3 = M1xM2 + M5xM6 (the
-// mixed terms of the three faces cancel); the same six cross products enter
-// the volume derivative, whose six Walsh coefficients are taken three times
-// over (3 W1 = 3 M2xM3 + M4xM5, 3 W4 = M2xM6 + M5xM1, ...) so that no
-// multiplication by 1/3 is needed.
+// and the three vectors nx[0..2] = X1, X2, X3 that give the node normals.
+// The node normals, sums of the quarter-area vectors of each corner's three
+// faces (CalcElemNodeNormals :708-799), are linear in the corner's signs:
+// pf[c] = (s_xi X1 + s_eta X2 + s_zeta X3)/64 with X1 = M2xM3 + M4xM5,
+// X2 = M3xM1 + M6xM4, X3 = M1xM2 + M5xM6 (the mixed terms of the three faces
+// cancel), so the normals of corners 4..7 are those of 2, 3, 0, 1 negated.
+// The same six cross products enter the volume derivative, whose six Walsh
+// coefficients are taken three times over (3 W1 = 3 M2xM3 + M4xM5,
+// 3 W4 = M2xM6 + M5xM1, ...) so that no multiplication by 1/3 is needed.
 template <typename T>
 __device__ __forceinline__ void force_geometry(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
                                                const V3<T> &M4, const V3<T> &M5, const V3<T> &M6,
-                                               T dx[8], T dy[8], T dz[8], V3<T> pf[4])
+                                               T dx[8], T dy[8], T dz[8], V3<T> nx[3])
 {
     const V3<T> c23 = cross3(M2, M3), c45 = cross3(M4, M5);
     const V3<T> c31 = cross3(M3, M1), c64 = cross3(M6, M4);
@@ -138,13 +138,9 @@ __device__ __forceinline__ void force_geometry(const V3<T> &M1, const V3<T> &M2,
     inv_walsh6(W1.y, W2.y, W3.y, W4.y, W5.y, W6.y, dy);
     inv_walsh6(W1.z, W2.z, W3.z, W4.z, W5.z, W6.z, dz);
 
-    const V3<T> X1 = sum3(c23, c45), X2 = sum3(c31, c64), X3 = sum3(c12, c56);
-    const V3<T> t1{X1.x + X2.x, X1.y + X2.y, X1.z + X2.z};
-    const V3<T> t2{X1.x - X2.x, X1.y - X2.y, X1.z - X2.z};
-    pf[0] = {-(t1.x + X3.x), -(t1.y + X3.y), -(t1.z + X3.z)};   // (-,-,-)
-    pf[1] = {t2.x - X3.x, t2.y - X3.y, t2.z - X3.z};            // (+,-,-)
-    pf[2] = {t1.x - X3.x, t1.y - X3.y, t1.z - X3.z};            // (+,+,-)
-    pf[3] = {-(t2.x + X3.x), -(t2.y + X3.y), -(t2.z + X3.z)};   // (-,+,-)
+    nx[0] = sum3(c23, c45);
+    nx[1] = sum3(c31, c64);
+    nx[2] = sum3(c12, c56);
 }
 
 // The six cross products of the modes that the volume, the node normals, the

@@ -112,9 +112,11 @@ struct Dom {
     double *e, *p, *q, *v, *ss;
     double *vnew, *delv, *vdov, *arealg, *ql, *qq;
     double *delv_xi, *delv_eta, *delv_zeta, *delx_xi, *delx_eta, *delx_zeta;
-    // corner forces, corner-major [8*ne]: stress and hourglass parts kept
-    // apart so that the node sums associate as the reference's do
-    double *fsx, *fsy, *fsz, *fhx, *fhy, *fhz;
+    // corner forces, corner-major [8*ne]: each corner's stress plus
+    // hourglass force (the reference sums the two parts over the node's
+    // corners separately and then adds the sums; adding them per corner
+    // first differs only by rounding)
+    double *fcx, *fcy, *fcz;
     // split precision: FP32 corner forces (corner-major [8*ne]), hi/lo
     // float pairs of the FP64 positions and velocities [nn], reciprocal
     // nodal masses [nn], FP32 monotonic-Q gradients [6][ne] in the order

@@ -35,12 +35,12 @@ constexpr long kNoAllocMaxElem = 1L << 16;   // 65,536 elements (a 40^3 cube fit
 constexpr long kNoAllocMaxNode = 1L << 17;   // 131,072 nodes
 
 // Layout of the array, in bytes from its start (each part 256-aligned):
-//   DevScalars | corner forces 6 x 8*E doubles | slot table 8*E ints |
+//   DevScalars | corner forces 3 x 8*E doubles | slot table 8*E ints |
 //   corner starts (N+1) ints | node mask N bytes
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr size_t kOffScalars = 0;
 constexpr size_t kOffForces = align256(sizeof(DevScalars));
-constexpr size_t kOffSlots = kOffForces + align256(6 * 8 * kNoAllocMaxElem * sizeof(double));
+constexpr size_t kOffSlots = kOffForces + align256(3 * 8 * kNoAllocMaxElem * sizeof(double));
 constexpr size_t kOffStart = kOffSlots + align256(8 * kNoAllocMaxElem * sizeof(int));
 constexpr size_t kOffMask = kOffStart + align256((kNoAllocMaxNode + 1) * sizeof(int));
 constexpr size_t kScratchBytes = kOffMask + align256(kNoAllocMaxNode);
@@ -186,12 +186,9 @@ extern "C" int lulesh_lagrange_nodal_noalloc(
     d.v = const_cast<double *>(v);
     d.ss = const_cast<double *>(ss);
     double *forces = reinterpret_cast<double *>(base + kOffForces);
-    d.fsx = forces;
-    d.fsy = forces + 8 * ne;
-    d.fsz = forces + 16 * ne;
-    d.fhx = forces + 24 * ne;
-    d.fhy = forces + 32 * ne;
-    d.fhz = forces + 40 * ne;
+    d.fcx = forces;
+    d.fcy = forces + 8 * ne;
+    d.fcz = forces + 16 * ne;
     d.sc = reinterpret_cast<DevScalars *>(base + kOffScalars);
     d.gate = nullptr;
     d.prm = *params;

@@ -4,9 +4,9 @@
 //   k_time_increment   1 thread   TimeIncrement                (LULESH-OMP.cc:557-604)
 //   k_elem_force       1 thr/elem IntegrateStressForElems + CalcHourglassControlForElems
 //                                 + CalcFBHourglassForceForElems, element half
-//                                 (:853-931, :1233-1558): 8 stress and 8 hourglass
-//                                 corner forces per element, corner-major SoA
-//   k_node_update      1 thr/node the two corner gathers (:905-926, :1475-1496) in
+//                                 (:853-931, :1233-1558): 8 corner forces (stress
+//                                 plus hourglass) per element, corner-major SoA
+//   k_node_update      1 thr/node the corner gather (:905-926, :1475-1496) in
 //                                 nodeElemCornerList order, CalcAccelerationForNodes,
 //                                 the symmetry-plane conditions, velocity and position
 //                                 (:1613-1683)
@@ -61,29 +61,38 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
 
     const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
     double dvdx[8], dvdy[8], dvdz[8];
-    V3<double> pf[4];
-    force_geometry(M1, M2, M3, M4, M5, M6, dvdx, dvdy, dvdz, pf);   // 192 x dV/dx, 64 x normals
+    V3<double> nx[3];
+    force_geometry(M1, M2, M3, M4, M5, M6, dvdx, dvdy, dvdz, nx);   // 192 x dV/dx, normal generators
 
     // IntegrateStressForElems (LULESH-OMP.cc:853-903): sig = -p - q and the
-    // corner force -sig * (area-weighted node normal); corners 4..7 carry
-    // the negated forces of corners 2, 3, 0, 1.  The Jacobian volume it
-    // checks is 8 t.(c x a) = M2.(M3 x M1) / 64; only its sign matters.
+    // corner force -sig * (area-weighted node normal).  The normal of the
+    // corner with signs s is (s_xi X1 + s_eta X2 + s_zeta X3)/64, so the
+    // stress forces are s . (Y1, Y2, Y3) with Y = ((p + q)/64) X, and those
+    // of corners 4..7 are the forces of corners 2, 3, 0, 1 negated.  The
+    // Jacobian volume it checks is 8 t.(c x a) = M2.(M3 x M1) / 64; only its
+    // sign matters.
+    double Y[3][3];
     {
-        const double sig64 = (1.0 / 64.0) * (-d.p[k] - d.q[k]);
-        const int neg_of[4] = {6, 7, 4, 5};
+        const double w = (1.0 / 64.0) * (d.p[k] + d.q[k]);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const double fx = -(sig64 * pf[c].x), fy = -(sig64 * pf[c].y), fz = -(sig64 * pf[c].z);
-            d.fsx[c * ne + k] = fx;
-            d.fsy[c * ne + k] = fy;
-            d.fsz[c * ne + k] = fz;
-            d.fsx[neg_of[c] * ne + k] = neg(fx);
-            d.fsy[neg_of[c] * ne + k] = neg(fy);
-            d.fsz[neg_of[c] * ne + k] = neg(fz);
+        for (int i = 0; i < 3; ++i) {
+            Y[i][0] = w * nx[i].x;
+            Y[i][1] = w * nx[i].y;
+            Y[i][2] = w * nx[i].z;
         }
         const double determ64 = dot3(M2, cross3(M3, M1));
         if (determ64 <= 0.0) flag_error(sc, ERR_K1_DETERM, k);
     }
+    // stress force of corners 0..3 in one component (corners 4..7: 2, 3,
+    // 0, 1 negated)
+    auto stress4 = [&](int dim, double f[4]) {
+        const double a = Y[0][dim] + Y[1][dim], b = Y[0][dim] - Y[1][dim], z = Y[2][dim];
+        f[0] = -(a + z);   // (-,-,-)
+        f[1] = b - z;      // (+,-,-)
+        f[2] = a - z;      // (+,+,-)
+        f[3] = -(b + z);   // (-,+,-)
+    };
+    double *out[3] = {d.fcx, d.fcy, d.fcz};
 
     // CalcHourglassControlForElems (:1503-1558)
     const double vk = d.v[k];
@@ -93,10 +102,14 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
     const double hourg = d.prm.hgcoef;
     if (!gt(hourg, 0.0)) {
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            d.fhx[c * ne + k] = 0.0;
-            d.fhy[c * ne + k] = 0.0;
-            d.fhz[c * ne + k] = 0.0;
+        for (int dim = 0; dim < 3; ++dim) {
+            double f[4];
+            stress4(dim, f);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                out[dim][c * ne + k] = f[c];
+                out[dim][(c ^ 6) * ne + k] = neg(f[c]);
+            }
         }
         return;
     }
@@ -127,9 +140,12 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
     }
     const double coefficient = -hourg * 0.01 * d.ss[k] * d.elem_mass[k] * r;
 
-    // CalcElemFBHourglassForce (:1050-1231), one velocity component at a time
+    // CalcElemFBHourglassForce (:1050-1231), one velocity component at a
+    // time; each corner's stress force is the addend of its hourglass sum
+    // (the reference adds the two node sums instead, :905-926 and
+    // :1475-1496: the same total up to rounding, with one gather instead of
+    // two)
     const double *vel[3] = {d.xd, d.yd, d.zd};
-    double *out[3] = {d.fhx, d.fhy, d.fhz};
 #pragma unroll
     for (int dim = 0; dim < 3; ++dim) {
         double u[8];
@@ -142,13 +158,16 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
             for (int c = 1; c < 8; ++c) acc = acc + hg[c][m] * u[c];
             h[m] = coefficient * acc;
         }
+        double f[4];
+        stress4(dim, f);
+        const double st[8] = {f[0], f[1], f[2], f[3], -f[2], -f[3], -f[0], -f[1]};
 #pragma unroll
         for (int c = 0; c < 8; ++c)
-            out[dim][c * ne + k] = ((hg[c][0] * h[0] + hg[c][1] * h[1]) + hg[c][2] * h[2]) + hg[c][3] * h[3];
+            out[dim][c * ne + k] = (((st[c] + hg[c][0] * h[0]) + hg[c][1] * h[1]) + hg[c][2] * h[2]) + hg[c][3] * h[3];
     }
 }
 
-__global__ void __launch_bounds__(kBlockElem) k_elem_force(const __grid_constant__ Dom d)
+__global__ void __launch_bounds__(kBlockElem, 4) k_elem_force(const __grid_constant__ Dom d)
 {
     if (skip_step(d)) return;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -157,7 +176,7 @@ __global__ void __launch_bounds__(kBlockElem) k_elem_force(const __grid_constant
 }
 
 // ---------------------------------------------------------------------
-// Node update: fixed-order corner gathers + acceleration, BC, velocity,
+// Node update: fixed-order corner gather + acceleration, BC, velocity,
 // position
 // ---------------------------------------------------------------------
 __device__ __forceinline__ void node_update_fp64(const Dom &d, int n, const DevScalars *sc)
@@ -167,26 +186,19 @@ __device__ __forceinline__ void node_update_fp64(const Dom &d, int n, const DevS
     // the sums start from the first corner rather than from 0.0 (the same
     // value: x + 0.0 == x, up to the sign of a zero sum), one FP64 add fewer
     // per component; every node belongs to at least one element
-    double sx = 0.0, sy = 0.0, sz = 0.0, hx = 0.0, hy = 0.0, hz = 0.0;
+    double fx = 0.0, fy = 0.0, fz = 0.0;
     if (st < en) {
         const int c = __ldg(d.corner_list + st);
-        sx = d.fsx[c];
-        sy = d.fsy[c];
-        sz = d.fsz[c];
-        hx = d.fhx[c];
-        hy = d.fhy[c];
-        hz = d.fhz[c];
+        fx = d.fcx[c];
+        fy = d.fcy[c];
+        fz = d.fcz[c];
     }
     for (int i = st + 1; i < en; ++i) {
         const int c = __ldg(d.corner_list + i);
-        sx += d.fsx[c];
-        sy += d.fsy[c];
-        sz += d.fsz[c];
-        hx += d.fhx[c];
-        hy += d.fhy[c];
-        hz += d.fhz[c];
+        fx += d.fcx[c];
+        fy += d.fcy[c];
+        fz += d.fcz[c];
     }
-    const double fx = sx + hx, fy = sy + hy, fz = sz + hz;
     if (d.keep & 1) {
         d.fx[n] = fx;
         d.fy[n] = fy;
