@@ -283,11 +283,13 @@ int lulesh_probe_fp64_peak(double *tflops);
  * conversion (each paired with one FP64 add), rates[3] FP64 division. */
 int lulesh_probe_pipe_rates(double *rates);
 
-/* Accuracy of the library's own FP64 root functions against CUDA's, over
- * 2^20 arguments spread over [2^-60, 2^60]: errs[0] the largest relative
- * difference of the inverse cube root (hourglass coefficient) from rcbrt,
- * errs[1] that of x*rsqrt(x) (sound speed) from sqrt. */
-int lulesh_probe_math(double errs[2]);
+/* Accuracy of the library's own FP64 root and reciprocal functions against
+ * CUDA's, over 2^20 arguments spread over [2^-140, 2^140]: the largest
+ * relative difference of errs[0] the inverse cube root (hourglass
+ * coefficient) from rcbrt, errs[1] x*rsqrt(x) (sound speed) from sqrt,
+ * errs[2] the reciprocal (compressions, Q limiter) from __drcp_rn, errs[3]
+ * the quotient (strain rate, density, hydro constraint) from a / x. */
+int lulesh_probe_math(double errs[4]);
 
 /* ---- LagrangeNodal without allocation ---------------------------------
  * No counterpart in the reference: an addition for callers that cannot

@@ -645,11 +645,12 @@ def probe_fp64_peak() -> float:
 
 
 def probe_math() -> dict:
-    """Largest relative differences of the library's inverse cube root and
-    square root from CUDA's rcbrt and sqrt."""
-    e = np.zeros(2)
+    """Largest relative differences of the library's inverse cube root,
+    square root, reciprocal and quotient from CUDA's rcbrt, sqrt, __drcp_rn
+    and division."""
+    e = np.zeros(4)
     _check(load_library().lulesh_probe_math(_ptr(e)))
-    return {"inv_cbrt_vs_rcbrt": float(e[0]), "x_rsqrt_x_vs_sqrt": float(e[1])}
+    return dict(zip(("rcbrt", "sqrt", "rcp", "quot"), e.tolist()))
 
 
 def probe_pipe_rates() -> dict:

@@ -865,10 +865,10 @@ int lulesh_probe_fp64_peak(double *tflops)
     return LULESH_OK;
 }
 
-int lulesh_probe_math(double errs[2])
+int lulesh_probe_math(double errs[4])
 {
     if (!errs) return LULESH_ERR_ARG;
-    unsigned long long *keys = nullptr, h[2] = {0, 0};
+    unsigned long long *keys = nullptr, h[4] = {0, 0, 0, 0};
     cudaStream_t st = nullptr;
     const int n = 1 << 20;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
@@ -886,7 +886,7 @@ int lulesh_probe_math(double errs[2])
     cudaFree(keys);
     cudaStreamDestroy(st);
     if (e != cudaSuccess) return fail(nullptr, LULESH_ERR_CUDA, std::string("lulesh_probe_math: ") + cudaGetErrorString(e));
-    for (int i = 0; i < 2; ++i) std::memcpy(&errs[i], &h[i], sizeof(double));
+    for (int i = 0; i < 4; ++i) std::memcpy(&errs[i], &h[i], sizeof(double));
     return LULESH_OK;
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "lulesh_internal.h"
+#include "fastmath.cuh"
 
 #include <cuda_runtime.h>
 
@@ -109,8 +110,9 @@ __device__ __forceinline__ bool abs_lt(double a, double c) { return iabs(a) < ia
 __device__ __forceinline__ bool lt(float a, float b) { return a < b; }
 __device__ __forceinline__ bool gt(float a, float b) { return a > b; }
 
-// 1/x, correctly rounded in both precisions (the bits of a division).
-__device__ __forceinline__ double recip(double x) { return __drcp_rn(x); }
+// 1/x: in FP64 refined from the FP32 estimate (fastmath.cuh, within an ulp
+// or so of the quotient), in FP32 correctly rounded.
+__device__ __forceinline__ double recip(double x) { return rcp_fast(x); }
 __device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
 
 // Conversions between FP64 and FP32 run on GB300's FP64 pipe at the FP64
@@ -144,23 +146,6 @@ __device__ __forceinline__ double f2d(float f)
     if (fe == 0) return __longlong_as_double((long long)sign);
     const unsigned long long de = (fe == 0xff) ? 0x7ffULL : (unsigned long long)(fe - 127 + 1023);
     return __longlong_as_double((long long)(sign | (de << 52) | mant));
-}
-
-// d^(-1/3) for d > 0 by Newton's iteration on f(y) = y^-3 - d,
-// y <- y + y (1 - d y^3) / 3, from the FP32 estimate rcbrtf: each step
-// squares the relative error (2^-22 -> 2^-44 -> below FP64 rounding), so two
-// steps give the root to a few ulps with ten FP64 operations.
-__device__ __forceinline__ double inv_cbrt(double d)
-{
-    const double third = 1.0 / 3.0;
-    double y = f2d(rcbrtf(d2f(d)));
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        const double y3 = (y * y) * y;
-        const double e = fma(-y3, d, 1.0);
-        y = fma(y * e, third, y);
-    }
-    return y;
 }
 
 // One direction of the monotonic limiter (:2198-2228).
@@ -287,10 +272,9 @@ __device__ __forceinline__ double material_update(const Dom &d, int k, DevScalar
             opaque(delvc); opaque(e_old); opaque(p_old); opaque(q_old); opaque(vnewc);
             opaque(qlin); opaque(qquad);
         }
-        // __drcp_rn is the correctly rounded reciprocal: the bits of 1. / x
-        double compression = __drcp_rn(vnewc) - 1.;
+        double compression = rcp_fast(vnewc) - 1.;
         const double vchalf = vnewc - delvc * .5;
-        double comp_half = __drcp_rn(vchalf) - 1.;
+        double comp_half = rcp_fast(vchalf) - 1.;
         // vhalf = 1 / (1 + comp_half) (:2460), which is vchalf, vnewc or 1 in the
         // three cases below; taken directly instead of through two divisions
         double vhalf = vchalf;
@@ -406,7 +390,7 @@ __device__ __forceinline__ void constraint_keys(double ss, double vdov, double a
         if (lt(vdov, 0.)) dtf = dtf + qqc2 * arealg * arealg * vdov * vdov;
         dtf = arealg * rsqrt(dtf);      // arealg / sqrt(dtf)
         kc = order_key(dtf);
-        kh = order_key(P.dvovmax / (fabs(vdov) + 1.e-20));
+        kh = order_key(quot_fast(P.dvovmax, fabs(vdov) + 1.e-20));
     }
 }
 

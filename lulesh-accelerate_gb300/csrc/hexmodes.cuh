@@ -25,6 +25,8 @@
 // elements, checked against the reference formulas).
 #pragma once
 
+#include "fastmath.cuh"
+
 namespace lulesh {
 
 template <typename T>
@@ -217,7 +219,7 @@ __device__ __forceinline__ T strain_rate(const V3<T> &M1, const V3<T> &M2, const
     const V3<T> cxi = cross3(B, C), cet = cross3(C, A), cze = cross3(A, B);
     const T num = (cxi.x * V1.x + cet.x * V2.x + cze.x * V3m.x) + (cxi.y * V1.y + cet.y * V2.y + cze.y * V3m.y) +
                   (cxi.z * V1.z + cet.z * V2.z + cze.z * V3m.z);
-    return num / dot3(B, cet);
+    return quot_fast(num, dot3(B, cet));
 }
 
 }  // namespace lulesh

@@ -117,7 +117,7 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
     // CalcFBHourglassForceForElems (:1291-1473): hourgam = gamma -
     // volinv * (dV/dx . hourmod), with hourmod the gamma projections of the
     // coordinates (modes M6, M5, M4, M7).
-    const double r = inv_cbrt(determ);                      // determ^(-1/3)
+    const double r = rcbrt_fast(determ);                    // determ^(-1/3)
     const double volinv192 = (r * r * r) * (1.0 / 192.0);   // the 1/192 of the derivative
     double hg[8][4];
     {
@@ -283,7 +283,7 @@ __device__ __forceinline__ void elem_kinematics_fp64(const Dom &d, int k, DevSca
     {
         const double ptiny = 1.e-36;
         const double vol = volo * rel;
-        const double norm = __drcp_rn(vol + ptiny);
+        const double norm = rcp_fast(vol + ptiny);
         const double vscale = 0.015625 * norm;           // (1/16) (1/4) norm
         const V3<double> &Az = X.c12, &Ax = X.c23, &Ae = X.c31;
         d.delx_zeta[k] = vol * rsqrt(0.00390625 * dot3(Az, Az) + ptiny);
@@ -343,7 +343,7 @@ __device__ __forceinline__ void elem_material_fp64(const Dom &d, int k, DevScala
             if (gt(dxi, 0.)) dxi = 0.;
             if (gt(deta, 0.)) deta = 0.;
             if (gt(dzeta, 0.)) dzeta = 0.;
-            const double rho = d.elem_mass[k] / (volo * vnew);
+            const double rho = quot_fast(d.elem_mass[k], volo * vnew);
             qlin = -P.qlc_monoq * rho *
                    ((dxi * (1. - phixi) + deta * (1. - phieta)) + dzeta * (1. - phizeta));
             qquad = P.qqc_monoq * rho *
@@ -511,22 +511,26 @@ void launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStre
     k_fp64_probe<<<blocks, threads, 0, st>>>(out, iters, 0.999999, 1e-7);
 }
 
-// Issue-rate probes for the design notes: 8 independent chains per thread
-// of one operation; each thread writes one value (keeps the chains live).
-// Arguments 2^(120 u - 60) (1 + v) over a grid of u, v; the relative
-// differences of inv_cbrt from rcbrt and of x*rsqrt(x) from sqrt, reduced as
-// the bit patterns of non-negative doubles (which order like the values).
+// Accuracy probe of the FP64 root and reciprocal functions against CUDA's.
+// Arguments 2^(280 u - 140) (1 + v) over a grid of u, v (both sides of the
+// range the fastmath.cuh functions refine, and its fallbacks); the relative
+// differences of rcbrt_fast from rcbrt, x*rsqrt(x) from sqrt, rcp_fast from
+// __drcp_rn and quot_fast(a, x) from a / x, reduced as the bit patterns of
+// non-negative doubles (which order like the values).
 __global__ void k_math_probe(unsigned long long *keys, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double u = (double)(i >> 10) / 1024.0, v = (double)(i & 1023) / 1024.0;
-    const double x = ldexp(1.0 + v, (int)(120.0 * u) - 60);
-    const double a = rcbrt(x), b = inv_cbrt(x);
-    const double s = sqrt(x), t = x * rsqrt(x);
-    const double ea = fabs(b - a) / a, es = fabs(t - s) / s;
-    atomicMax(keys, (unsigned long long)__double_as_longlong(ea));
-    atomicMax(keys + 1, (unsigned long long)__double_as_longlong(es));
+    const double x = ldexp(1.0 + v, (int)(280.0 * u) - 140);
+    const double num = (i & 1) ? -(1.0 + u) : 0.75 + v;
+    const double rel[4] = {
+        fabs(rcbrt_fast(x) - rcbrt(x)) / rcbrt(x),
+        fabs(x * rsqrt(x) - sqrt(x)) / sqrt(x),
+        fabs(rcp_fast(x) - __drcp_rn(x)) / __drcp_rn(x),
+        fabs(quot_fast(num, x) - num / x) / fabs(num / x)};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) atomicMax(keys + j, (unsigned long long)__double_as_longlong(rel[j]));
 }
 
 void launch_math_probe(unsigned long long *keys, int n, cudaStream_t st)
@@ -534,6 +538,8 @@ void launch_math_probe(unsigned long long *keys, int n, cudaStream_t st)
     k_math_probe<<<(n + 255) / 256, 256, 0, st>>>(keys, n);
 }
 
+// Issue-rate probes: 8 independent chains per thread of one operation; each
+// thread writes one value (keeps the chains live).
 __global__ void k_probe_ffma(float *out, int iters, float a, float b)
 {
     float r[8];
