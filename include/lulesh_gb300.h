@@ -336,8 +336,9 @@ int lulesh_lagrange_nodal_noalloc(
  * LULESH_INIT_V2 its initial time step is 0.5*cbrt(volo0)/sqrt(2*e0) of the
  * scaled energy.  Every instance's arithmetic is exactly that of a
  * single-instance context with the same initial state.  The batch runs as
- * one CUDA graph; per size class of instance (s <= 24, s <= 48, larger) each
- * step kernel has its own launch shape. */
+ * one CUDA graph; in split precision per size class of instance (s <= 24,
+ * s <= 48, larger) each step kernel has its own launch shape and the classes
+ * run as parallel branches, in FP64 all instances form one class. */
 typedef struct lulesh_batch lulesh_batch;
 
 int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int init_mode, int precision,
