@@ -46,6 +46,23 @@ __device__ __forceinline__ T dot3(const V3<T> &a, const V3<T> &b)
     return a.x * b.x + a.y * b.y + a.z * b.z;
 }
 
+// acc + a.b as one chain of three fused multiply-adds
+template <typename T>
+__device__ __forceinline__ T dot3_acc(const V3<T> &a, const V3<T> &b, T acc)
+{
+    return fma(a.z, b.z, fma(a.y, b.y, fma(a.x, b.x, acc)));
+}
+
+// a x b + c x d, four operations per component (one product and three
+// fused multiply-adds) instead of the five of two crosses and a sum
+template <typename T>
+__device__ __forceinline__ V3<T> cross_sum(const V3<T> &a, const V3<T> &b, const V3<T> &c, const V3<T> &d)
+{
+    return {fma(a.y, b.z, fma(-a.z, b.y, fma(c.y, d.z, -(c.z * d.y)))),
+            fma(a.z, b.x, fma(-a.x, b.z, fma(c.z, d.x, -(c.x * d.z)))),
+            fma(a.x, b.y, fma(-a.y, b.x, fma(c.x, d.y, -(c.y * d.x))))};
+}
+
 // Modes m[0..6] = M1..M7 (xi, eta, zeta, xi eta, xi zeta, eta zeta,
 // xi eta zeta) of 8 corner values.
 template <typename T>
@@ -133,9 +150,9 @@ __device__ __forceinline__ void force_geometry(const V3<T> &M1, const V3<T> &M2,
     const V3<T> W1 = add3(c23, T(3.0), c45);
     const V3<T> W2 = add3(c31, T(3.0), c64);
     const V3<T> W3 = add3(c12, T(3.0), c56);
-    const V3<T> W4 = sum3(cross3(M2, M6), cross3(M5, M1));
-    const V3<T> W5 = sum3(cross3(M6, M3), cross3(M1, M4));
-    const V3<T> W6 = sum3(cross3(M4, M2), cross3(M3, M5));
+    const V3<T> W4 = cross_sum(M2, M6, M5, M1);
+    const V3<T> W5 = cross_sum(M6, M3, M1, M4);
+    const V3<T> W6 = cross_sum(M4, M2, M3, M5);
     inv_walsh6(W1.x, W2.x, W3.x, W4.x, W5.x, W6.x, dx);
     inv_walsh6(W1.y, W2.y, W3.y, W4.y, W5.y, W6.y, dy);
     inv_walsh6(W1.z, W2.z, W3.z, W4.z, W5.z, W6.z, dz);
@@ -167,7 +184,7 @@ __device__ __forceinline__ T volume64_shared(const V3<T> &M1, const V3<T> &M2, c
                                              const ModeCrosses<T> &C)
 {
     const T third = T(1.0) / T(3.0);
-    return dot3(M1, C.c23) + ((dot3(M2, C.c64) + dot3(M3, C.c56)) + dot3(M1, C.c45)) * third;
+    return fma(dot3_acc(M1, C.c45, dot3_acc(M3, C.c56, dot3(M2, C.c64))), third, dot3(M1, C.c23));
 }
 
 // 64 x the largest |u x v|^2 over the six faces (u, v the face diagonals),
@@ -186,7 +203,7 @@ __device__ __forceinline__ T max_face_cross2_64(const V3<T> &M1, const V3<T> &M2
     auto pair = [](const V3<T> &p, const V3<T> &q, const V3<T> &r, const V3<T> &t, T sy) {
         const V3<T> X{p.x + q.x, p.y + q.y, p.z + q.z};
         const V3<T> Y{r.x + sy * t.x, r.y + sy * t.y, r.z + sy * t.z};
-        return (dot3(X, X) + dot3(Y, Y)) + T(2.0) * fabs(dot3(X, Y));
+        return fma(T(2.0), fabs(dot3(X, Y)), dot3_acc(Y, Y, dot3(X, X)));
     };
     const T f1 = pair(C.c23, C.c45, b, a, T(-1.0));   // Y1 = b - a
     const T f2 = pair(C.c31, C.c64, c, a, T(1.0));    // Y2 = c + a
@@ -217,8 +234,7 @@ __device__ __forceinline__ T strain_rate(const V3<T> &M1, const V3<T> &M2, const
     const V3<T> B{M2.x - dt2 * V2.x, M2.y - dt2 * V2.y, M2.z - dt2 * V2.z};
     const V3<T> C{M3.x - dt2 * V3m.x, M3.y - dt2 * V3m.y, M3.z - dt2 * V3m.z};
     const V3<T> cxi = cross3(B, C), cet = cross3(C, A), cze = cross3(A, B);
-    const T num = (cxi.x * V1.x + cet.x * V2.x + cze.x * V3m.x) + (cxi.y * V1.y + cet.y * V2.y + cze.y * V3m.y) +
-                  (cxi.z * V1.z + cet.z * V2.z + cze.z * V3m.z);
+    const T num = dot3_acc(cze, V3m, dot3_acc(cet, V2, dot3(cxi, V1)));
     return quot_fast(num, dot3(B, cet));
 }
 

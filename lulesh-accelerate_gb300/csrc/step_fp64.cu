@@ -283,8 +283,8 @@ __device__ __forceinline__ void elem_kinematics_fp64(const Dom &d, int k, DevSca
     {
         const double ptiny = 1.e-36;
         const double vol = volo * rel;
-        const double norm = rcp_fast(vol + ptiny);
-        const double vscale = 0.015625 * norm;           // (1/16) (1/4) norm
+        // (1/16) (1/4) / (vol + ptiny), the power-of-two scale taken inside
+        const double vscale = rcp_fast(fma(vol, 64.0, 64.0 * ptiny));
         const V3<double> &Az = X.c12, &Ax = X.c23, &Ae = X.c31;
         d.delx_zeta[k] = vol * rsqrt(0.00390625 * dot3(Az, Az) + ptiny);
         d.delv_zeta[k] = vscale * dot3(Az, V3v);
