@@ -87,17 +87,24 @@ __device__ __forceinline__ DF df_sum4(DF a, DF b, DF c, DF d)
 }
 
 __device__ __forceinline__ DF df_neg(DF a) { return {-a.hi, -a.lo}; }
-__device__ __forceinline__ double df_value(DF a) { return f2d(a.hi) + f2d(a.lo); }
+
+// hi + lo as the FP32 rounding of the sum and its exact remainder (Knuth's
+// two-sum), so that |lo| <= 2^-24 |hi|.
+__device__ __forceinline__ DF df_renorm(DF a)
+{
+    const float s = a.hi + a.lo;
+    const float bb = s - a.hi;
+    return {s, (a.hi - (s - bb)) + (a.lo - bb)};
+}
 
 // The Walsh modes M1..M6 of one coordinate of the 8 corners, from hi/lo
-// pairs, in FP64.  Every mode but the constant one is a signed sum of four
-// edge differences (M1 = a+b+c+d, M4 = -a+b-c+d, M5 = -a-b+c+d over the xi
-// edges a..d; M2 = p+q+r+t, M6 = -p-q+r+t over the eta edges; M3 over the
-// zeta edges), so the sums run on small, exactly formed differences in
-// compensated FP32 and only the six results are converted and added in
-// FP64.  With linear_only, M1..M3 alone.
+// pairs, as renormalised hi/lo pairs.  Every mode but the constant one is a
+// signed sum of four edge differences (M1 = a+b+c+d, M4 = -a+b-c+d,
+// M5 = -a-b+c+d over the xi edges a..d; M2 = p+q+r+t, M6 = -p-q+r+t over the
+// eta edges; M3 over the zeta edges), so the sums run on small, exactly
+// formed differences in compensated FP32.  With linear_only, M1..M3 alone.
 template <bool kLinearOnly>
-__device__ __forceinline__ void df_modes(const float2 *__restrict__ f, const int nl[8], double m[6])
+__device__ __forceinline__ void df_modes(const float2 *__restrict__ f, const int nl[8], DF m[6])
 {
     float2 c[8];
 #pragma unroll
@@ -105,14 +112,79 @@ __device__ __forceinline__ void df_modes(const float2 *__restrict__ f, const int
     const DF a = df_diff(c[1], c[0]), b = df_diff(c[2], c[3]), cc = df_diff(c[5], c[4]), dd = df_diff(c[6], c[7]);
     const DF p = df_diff(c[3], c[0]), q = df_diff(c[2], c[1]), r = df_diff(c[7], c[4]), t = df_diff(c[6], c[5]);
     const DF u = df_diff(c[4], c[0]), v = df_diff(c[5], c[1]), w = df_diff(c[6], c[2]), z = df_diff(c[7], c[3]);
-    m[0] = df_value(df_sum4(a, b, cc, dd));
-    m[1] = df_value(df_sum4(p, q, r, t));
-    m[2] = df_value(df_sum4(u, v, w, z));
+    m[0] = df_renorm(df_sum4(a, b, cc, dd));
+    m[1] = df_renorm(df_sum4(p, q, r, t));
+    m[2] = df_renorm(df_sum4(u, v, w, z));
     if (!kLinearOnly) {
-        m[3] = df_value(df_sum4(df_neg(a), b, df_neg(cc), dd));
-        m[4] = df_value(df_sum4(df_neg(a), df_neg(b), cc, dd));
-        m[5] = df_value(df_sum4(df_neg(p), df_neg(q), r, t));
+        m[3] = df_renorm(df_sum4(df_neg(a), b, df_neg(cc), dd));
+        m[4] = df_renorm(df_sum4(df_neg(a), df_neg(b), cc, dd));
+        m[5] = df_renorm(df_sum4(df_neg(p), df_neg(q), r, t));
     }
+}
+
+// Mode i of the three coordinates: hi words (FP32), as FP64 (exact), and
+// lo words.
+struct ModeSplit {
+    V3<float> hi, lo;
+    V3<double> hd;
+};
+__device__ __forceinline__ ModeSplit mode_split(const DF mx[6], const DF my[6], const DF mz[6], int i)
+{
+    return {{mx[i].hi, my[i].hi, mz[i].hi}, {mx[i].lo, my[i].lo, mz[i].lo},
+            {f2d(mx[i].hi), f2d(my[i].hi), f2d(mz[i].hi)}};
+}
+
+// 64 x the relative volume change for the lo words, to first order: the
+// volume formula of hexmodes.cuh has the gradient dV64/dM_i = W_i / 3 with
+// W1 = 3 M2xM3 + M4xM5, W2 = 3 M3xM1 + M6xM4, W3 = 3 M1xM2 + M5xM6,
+// W4 = M2xM6 + M5xM1, W5 = M6xM3 + M1xM4, W6 = M4xM2 + M3xM5 (the same
+// vectors as the volume derivative of force_geometry), in FP32 on the hi
+// words.
+__device__ __forceinline__ float volume64_correction(const ModeSplit M[6])
+{
+    const V3<float> &M1 = M[0].hi, &M2 = M[1].hi, &M3 = M[2].hi, &M4 = M[3].hi, &M5 = M[4].hi, &M6 = M[5].hi;
+    auto w3 = [](const V3<float> &c, const V3<float> &e) {
+        return V3<float>{fmaf(3.f, c.x, e.x), fmaf(3.f, c.y, e.y), fmaf(3.f, c.z, e.z)};
+    };
+    const V3<float> W[6] = {w3(cross3(M2, M3), cross3(M4, M5)), w3(cross3(M3, M1), cross3(M6, M4)),
+                            w3(cross3(M1, M2), cross3(M5, M6)), cross_sum(M2, M6, M5, M1),
+                            cross_sum(M6, M3, M1, M4), cross_sum(M4, M2, M3, M5)};
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s = dot3_acc(M[i].lo, W[i], s);
+    return s * (1.f / 3.f);
+}
+
+// The half-step strain rate (strain_rate of hexmodes.cuh) in FP64 on the hi
+// words of the position and velocity modes, with its numerator and
+// denominator corrected to first order for the lo words in FP32.
+__device__ __forceinline__ double strain_rate_split(const ModeSplit M[3], const ModeSplit V[3], double dt2)
+{
+    const V3<double> A{fma(-dt2, V[0].hd.x, M[0].hd.x), fma(-dt2, V[0].hd.y, M[0].hd.y), fma(-dt2, V[0].hd.z, M[0].hd.z)};
+    const V3<double> B{fma(-dt2, V[1].hd.x, M[1].hd.x), fma(-dt2, V[1].hd.y, M[1].hd.y), fma(-dt2, V[1].hd.z, M[1].hd.z)};
+    const V3<double> C{fma(-dt2, V[2].hd.x, M[2].hd.x), fma(-dt2, V[2].hd.y, M[2].hd.y), fma(-dt2, V[2].hd.z, M[2].hd.z)};
+    const V3<double> cxi = cross3(B, C), cet = cross3(C, A), cze = cross3(A, B);
+    const double num = dot3_acc(cze, V[2].hd, dot3_acc(cet, V[1].hd, dot3(cxi, V[0].hd)));
+    const double den = dot3(B, cet);
+
+    // FP32: the same quantities on the hi words, and the lo words' changes
+    // a, b, c of A, B, C; d(den) = a.(BxC) + b.(CxA) + c.(AxB),
+    // d(num) = d(BxC).V1 + d(CxA).V2 + d(AxB).V3 + (BxC).v1 + (CxA).v2 + (AxB).v3
+    const float h = d2f(dt2);
+    auto half = [h](const V3<float> &m, const V3<float> &v) {
+        return V3<float>{fmaf(-h, v.x, m.x), fmaf(-h, v.y, m.y), fmaf(-h, v.z, m.z)};
+    };
+    const V3<float> Af = half(M[0].hi, V[0].hi), Bf = half(M[1].hi, V[1].hi), Cf = half(M[2].hi, V[2].hi);
+    const V3<float> a = half(M[0].lo, V[0].lo), b = half(M[1].lo, V[1].lo), c = half(M[2].lo, V[2].lo);
+    const V3<float> fxi = cross3(Bf, Cf), fet = cross3(Cf, Af), fze = cross3(Af, Bf);
+    const float dden = dot3_acc(c, fze, dot3_acc(b, fet, dot3(a, fxi)));
+    float dnum = dot3(cross_sum(b, Cf, Bf, c), V[0].hi);
+    dnum = dot3_acc(cross_sum(c, Af, Cf, a), V[1].hi, dnum);
+    dnum = dot3_acc(cross_sum(a, Bf, Af, b), V[2].hi, dnum);
+    dnum = dot3_acc(fxi, V[0].lo, dnum);
+    dnum = dot3_acc(fet, V[1].lo, dnum);
+    dnum = dot3_acc(fze, V[2].lo, dnum);
+    return quot_fast(num + f2d(dnum), den + f2d(dden));
 }
 
 // FP64 state -> hi/lo pairs and reciprocal masses (after any host upload).
@@ -305,24 +377,32 @@ __device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevSc
     // FP64: relative volume and the half-step strain rate through the Walsh
     // modes of the corner coordinates and velocities (CalcKinematicsForElems
     // :1950-1958, :1975-2020; the identities of hexmodes.cuh).  The modes
-    // come from the hi/lo pairs by compensated FP32 edge sums (df_modes);
-    // cross products, volume, strain rate and the divisions are FP64.
-    const double volo = d.volo[k];
+    // come from the hi/lo pairs by compensated FP32 edge sums (df_modes) as
+    // hi + lo with |lo| <= 2^-24 |hi|.  Cross products, volume, strain rate
+    // and the division are FP64 on the hi words (exact in FP64); the lo
+    // words enter through first-order corrections formed in FP32, whose
+    // rounding and neglected second-order terms stay near 2^-47 of the
+    // value, below the ~2^-45 the compensated sums carry.
     double volume, vdov;
     {
-        double mx[6], my[6], mz[6];
+        DF mx[6], my[6], mz[6];
         df_modes<false>(d.xs, nl, mx);
         df_modes<false>(d.ys, nl, my);
         df_modes<false>(d.zs, nl, mz);
-        const V3<double> M1 = mode(mx, my, mz, 0), M2 = mode(mx, my, mz, 1), M3 = mode(mx, my, mz, 2);
-        const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
-        volume = volume64_shared(M1, M2, M3, mode_crosses(M1, M2, M3, M4, M5, M6)) * (1.0 / 64.0);
-        double vx[6], vy[6], vz[6];
+        ModeSplit M[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) M[i] = mode_split(mx, my, mz, i);
+        const double vol64 = volume64_shared(M[0].hd, M[1].hd, M[2].hd,
+                                             mode_crosses(M[0].hd, M[1].hd, M[2].hd, M[3].hd, M[4].hd, M[5].hd));
+        volume = (vol64 + f2d(volume64_correction(M))) * (1.0 / 64.0);
+        DF vx[6], vy[6], vz[6];
         df_modes<true>(d.xds, nl, vx);
         df_modes<true>(d.yds, nl, vy);
         df_modes<true>(d.zds, nl, vz);
-        vdov = strain_rate(M1, M2, M3, V3<double>{vx[0], vy[0], vz[0]}, V3<double>{vx[1], vy[1], vz[1]},
-                           V3<double>{vx[2], vy[2], vz[2]}, 0.5 * sc->deltatime);
+        ModeSplit V[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) V[i] = mode_split(vx, vy, vz, i);
+        vdov = strain_rate_split(M, V, 0.5 * sc->deltatime);
     }
     // volume / volo, as a product with the reciprocal taken at set-up (within
     // an ulp of the quotient)
