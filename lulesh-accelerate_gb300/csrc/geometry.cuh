@@ -114,32 +114,4 @@ __device__ __forceinline__ void volume_derivative(T dvdx[8], T dvdy[8], T dvdz[8
     volu_der(x, y, z, 6, 5, 4, 3, 2, 0, dvdx[7], dvdy[7], dvdz[7]);
 }
 
-// AreaFace (LULESH-OMP.cc:1799-1819).
-template <typename T>
-__device__ __forceinline__ T area_face(const T x[8], const T y[8], const T z[8], int a, int b, int c, int d)
-{
-    const T fx = (x[c] - x[a]) - (x[d] - x[b]);
-    const T fy = (y[c] - y[a]) - (y[d] - y[b]);
-    const T fz = (z[c] - z[a]) - (z[d] - z[b]);
-    const T gx = (x[c] - x[a]) + (x[d] - x[b]);
-    const T gy = (y[c] - y[a]) + (y[d] - y[b]);
-    const T gz = (z[c] - z[a]) + (z[d] - z[b]);
-    const T fg = fx * gx + fy * gy + fz * gz;
-    return (fx * fx + fy * fy + fz * fz) * (gx * gx + gy * gy + gz * gz) - fg * fg;
-}
-
-// CalcElemCharacteristicLength (LULESH-OMP.cc:1821-1862).
-template <typename T>
-__device__ __forceinline__ T char_length(const T x[8], const T y[8], const T z[8], T volume)
-{
-    T m = T(0.0), a;
-    a = area_face(x, y, z, 0, 1, 2, 3); m = fmax(a, m);
-    a = area_face(x, y, z, 4, 5, 6, 7); m = fmax(a, m);
-    a = area_face(x, y, z, 0, 1, 5, 4); m = fmax(a, m);
-    a = area_face(x, y, z, 1, 2, 6, 5); m = fmax(a, m);
-    a = area_face(x, y, z, 2, 3, 7, 6); m = fmax(a, m);
-    a = area_face(x, y, z, 3, 0, 4, 7); m = fmax(a, m);
-    return T(4.0) * volume / sqrt(m);
-}
-
 }  // namespace lulesh

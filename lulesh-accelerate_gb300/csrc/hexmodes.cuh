@@ -34,16 +34,21 @@ struct V3 {
     T x, y, z;
 };
 
+// The products and sums below are written as explicit fused multiply-adds,
+// so that every kernel that inlines them rounds the same way: the compiler
+// is otherwise free to fuse either product of a*b - c*d into the add, and
+// its choice may differ between a single-instance kernel and the batched
+// kernel that runs the same element body.
 template <typename T>
 __device__ __forceinline__ V3<T> cross3(const V3<T> &a, const V3<T> &b)
 {
-    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return {fma(a.y, b.z, -(a.z * b.y)), fma(a.z, b.x, -(a.x * b.z)), fma(a.x, b.y, -(a.y * b.x))};
 }
 
 template <typename T>
 __device__ __forceinline__ T dot3(const V3<T> &a, const V3<T> &b)
 {
-    return a.x * b.x + a.y * b.y + a.z * b.z;
+    return fma(a.z, b.z, fma(a.y, b.y, a.x * b.x));
 }
 
 // acc + a.b as one chain of three fused multiply-adds
@@ -202,7 +207,7 @@ __device__ __forceinline__ T max_face_cross2_64(const V3<T> &M1, const V3<T> &M2
     const V3<T> a = cross3(M3, M4), b = cross3(M2, M5), c = cross3(M6, M1);
     auto pair = [](const V3<T> &p, const V3<T> &q, const V3<T> &r, const V3<T> &t, T sy) {
         const V3<T> X{p.x + q.x, p.y + q.y, p.z + q.z};
-        const V3<T> Y{r.x + sy * t.x, r.y + sy * t.y, r.z + sy * t.z};
+        const V3<T> Y{fma(sy, t.x, r.x), fma(sy, t.y, r.y), fma(sy, t.z, r.z)};
         return fma(T(2.0), fabs(dot3(X, Y)), dot3_acc(Y, Y, dot3(X, X)));
     };
     const T f1 = pair(C.c23, C.c45, b, a, T(-1.0));   // Y1 = b - a

@@ -139,15 +139,14 @@ __device__ __forceinline__ ModeSplit mode_split(const DF mx[6], const DF my[6], 
 // W1 = 3 M2xM3 + M4xM5, W2 = 3 M3xM1 + M6xM4, W3 = 3 M1xM2 + M5xM6,
 // W4 = M2xM6 + M5xM1, W5 = M6xM3 + M1xM4, W6 = M4xM2 + M3xM5 (the same
 // vectors as the volume derivative of force_geometry), in FP32 on the hi
-// words.
-__device__ __forceinline__ float volume64_correction(const ModeSplit M[6])
+// words, whose shared cross products are C.
+__device__ __forceinline__ float volume64_correction(const ModeSplit M[6], const ModeCrosses<float> &C)
 {
     const V3<float> &M1 = M[0].hi, &M2 = M[1].hi, &M3 = M[2].hi, &M4 = M[3].hi, &M5 = M[4].hi, &M6 = M[5].hi;
     auto w3 = [](const V3<float> &c, const V3<float> &e) {
         return V3<float>{fmaf(3.f, c.x, e.x), fmaf(3.f, c.y, e.y), fmaf(3.f, c.z, e.z)};
     };
-    const V3<float> W[6] = {w3(cross3(M2, M3), cross3(M4, M5)), w3(cross3(M3, M1), cross3(M6, M4)),
-                            w3(cross3(M1, M2), cross3(M5, M6)), cross_sum(M2, M6, M5, M1),
+    const V3<float> W[6] = {w3(C.c23, C.c45), w3(C.c31, C.c64), w3(C.c12, C.c56), cross_sum(M2, M6, M5, M1),
                             cross_sum(M6, M3, M1, M4), cross_sum(M4, M2, M3, M5)};
     float s = 0.f;
 #pragma unroll
@@ -365,8 +364,6 @@ __global__ void __launch_bounds__(kBlockNode) k_node_update_split(const __grid_c
 // Element kinematics: FP64 volume and strain rate, FP32 length and Q
 // gradients
 // ---------------------------------------------------------------------
-__device__ __forceinline__ float sum4f(float a, float b, float c, float e) { return ((a + b) + c) + e; }
-
 __device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevScalars *sc)
 {
     const size_t ne = (size_t)d.ne;
@@ -383,85 +380,56 @@ __device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevSc
     // words enter through first-order corrections formed in FP32, whose
     // rounding and neglected second-order terms stay near 2^-47 of the
     // value, below the ~2^-45 the compensated sums carry.
-    double volume, vdov;
-    {
-        DF mx[6], my[6], mz[6];
-        df_modes<false>(d.xs, nl, mx);
-        df_modes<false>(d.ys, nl, my);
-        df_modes<false>(d.zs, nl, mz);
-        ModeSplit M[6];
+    DF mx[6], my[6], mz[6];
+    df_modes<false>(d.xs, nl, mx);
+    df_modes<false>(d.ys, nl, my);
+    df_modes<false>(d.zs, nl, mz);
+    ModeSplit M[6];
 #pragma unroll
-        for (int i = 0; i < 6; ++i) M[i] = mode_split(mx, my, mz, i);
-        const double vol64 = volume64_shared(M[0].hd, M[1].hd, M[2].hd,
-                                             mode_crosses(M[0].hd, M[1].hd, M[2].hd, M[3].hd, M[4].hd, M[5].hd));
-        volume = (vol64 + f2d(volume64_correction(M))) * (1.0 / 64.0);
-        DF vx[6], vy[6], vz[6];
-        df_modes<true>(d.xds, nl, vx);
-        df_modes<true>(d.yds, nl, vy);
-        df_modes<true>(d.zds, nl, vz);
-        ModeSplit V[3];
+    for (int i = 0; i < 6; ++i) M[i] = mode_split(mx, my, mz, i);
+    DF vx[6], vy[6], vz[6];
+    df_modes<true>(d.xds, nl, vx);
+    df_modes<true>(d.yds, nl, vy);
+    df_modes<true>(d.zds, nl, vz);
+    ModeSplit V[3];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) V[i] = mode_split(vx, vy, vz, i);
-        vdov = strain_rate_split(M, V, 0.5 * sc->deltatime);
-    }
+    for (int i = 0; i < 3; ++i) V[i] = mode_split(vx, vy, vz, i);
+    const ModeCrosses<float> Cf = mode_crosses(M[0].hi, M[1].hi, M[2].hi, M[3].hi, M[4].hi, M[5].hi);
+
+    const double vol64 = volume64_shared(M[0].hd, M[1].hd, M[2].hd,
+                                         mode_crosses(M[0].hd, M[1].hd, M[2].hd, M[3].hd, M[4].hd, M[5].hd));
+    const double volume = (vol64 + f2d(volume64_correction(M, Cf))) * (1.0 / 64.0);
     // volume / volo, as a product with the reciprocal taken at set-up (within
     // an ulp of the quotient)
     const double rel = volume * __ldg(d.inv_volo + k);
     d.vnew[k] = rel;
     d.delv[k] = rel - d.v[k];
-    d.vdov[k] = vdov;
+    d.vdov[k] = strain_rate_split(M, V, 0.5 * sc->deltatime);
     if (rel <= 0.0) flag_error(sc, ERR_K3_VNEW, k);
 
     // FP32: characteristic length and monotonic-Q gradients (:1821-1862,
-    // :2034-2180) on corner-0-relative coordinates
-    float x[8], y[8], z[8], xv[8], yv[8], zv[8];
-    rel8(d.xs, nl, x);
-    rel8(d.ys, nl, y);
-    rel8(d.zs, nl, z);
-    rel8(d.xds, nl, xv);
-    rel8(d.yds, nl, yv);
-    rel8(d.zds, nl, zv);
-    const float volf = d2f(volume);
-    d.arealg[k] = f2d(char_length<float>(x, y, z, volf));
-
-    const float ptiny = 1.e-36f;
+    // :2034-2180) through the hi words of the modes, with the formulas of the
+    // FP64 kernel (face areas from the shared cross products; the logical
+    // differences are M/4, so each cross product is (M x M')/16 and each
+    // velocity difference Mv/4)
     const float vol = d2f(volume);
-    const float norm = 1.f / (vol + ptiny);
-#define DJ(f) (-0.25f * (sum4f(f[0], f[1], f[5], f[4]) - sum4f(f[3], f[2], f[6], f[7])))
-#define DI(f) ( 0.25f * (sum4f(f[1], f[2], f[6], f[5]) - sum4f(f[0], f[3], f[7], f[4])))
-#define DK(f) ( 0.25f * (sum4f(f[4], f[5], f[6], f[7]) - sum4f(f[0], f[1], f[2], f[3])))
-    const float dxj = DJ(x), dyj = DJ(y), dzj = DJ(z);
-    const float dxi = DI(x), dyi = DI(y), dzi = DI(z);
-    const float dxk = DK(x), dyk = DK(y), dzk = DK(z);
-    float ax, ay, az;
+    d.arealg[k] = f2d((16.f * vol) * rsqrtf(max_face_cross2_64(M[0].hi, M[1].hi, M[2].hi, M[3].hi, M[4].hi, M[5].hi, Cf)));
+    const float ptiny = 1.e-36f;
+    const float vscale = 1.f / fmaf(vol, 64.f, 64.f * ptiny);     // (1/16) (1/4) / (vol + ptiny)
     float *gq = d.gq;
-
-    ax = dyi * dzj - dzi * dyj;
-    ay = dzi * dxj - dxi * dzj;
-    az = dxi * dyj - dyi * dxj;
-    gq[5 * ne + k] = vol / sqrtf(ax * ax + ay * ay + az * az + ptiny);           // delx_zeta
-    ax *= norm; ay *= norm; az *= norm;
-    gq[2 * ne + k] = ax * DK(xv) + ay * DK(yv) + az * DK(zv);                   // delv_zeta
-
-    ax = dyj * dzk - dzj * dyk;
-    ay = dzj * dxk - dxj * dzk;
-    az = dxj * dyk - dyj * dxk;
-    gq[3 * ne + k] = vol / sqrtf(ax * ax + ay * ay + az * az + ptiny);           // delx_xi
-    ax *= norm; ay *= norm; az *= norm;
-    gq[0 * ne + k] = ax * DI(xv) + ay * DI(yv) + az * DI(zv);                   // delv_xi
-
-    ax = dyk * dzi - dzk * dyi;
-    ay = dzk * dxi - dxk * dzi;
-    az = dxk * dyi - dyk * dxi;
-    gq[4 * ne + k] = vol / sqrtf(ax * ax + ay * ay + az * az + ptiny);           // delx_eta
-    ax *= norm; ay *= norm; az *= norm;
-    gq[1 * ne + k] = ax * DJ(xv) + ay * DJ(yv) + az * DJ(zv);                   // delv_eta
-#undef DJ
-#undef DI
-#undef DK
+    gq[5 * ne + k] = vol * rsqrtf(fmaf(0.00390625f, dot3(Cf.c12, Cf.c12), ptiny));   // delx_zeta
+    gq[2 * ne + k] = vscale * dot3(Cf.c12, V[2].hi);                                 // delv_zeta
+    gq[3 * ne + k] = vol * rsqrtf(fmaf(0.00390625f, dot3(Cf.c23, Cf.c23), ptiny));   // delx_xi
+    gq[0 * ne + k] = vscale * dot3(Cf.c23, V[0].hi);                                 // delv_xi
+    gq[4 * ne + k] = vol * rsqrtf(fmaf(0.00390625f, dot3(Cf.c31, Cf.c31), ptiny));   // delx_eta
+    gq[1 * ne + k] = vscale * dot3(Cf.c31, V[1].hi);                                 // delv_eta
 }
 
-__global__ void __launch_bounds__(kBlockElem) k_elem_kinematics_split(const __grid_constant__ Dom d)
+// Held to 96 registers (five blocks per SM; a few hundred bytes spilled):
+// with its FP64 work cut by the first-order corrections the kernel waits on
+// its corner gathers, and the extra resident block pays (1.27 -> 1.16 ms at
+// s=192 against the unbounded 128 registers).
+__global__ void __launch_bounds__(kBlockElem, 5) k_elem_kinematics_split(const __grid_constant__ Dom d)
 {
     if (skip_step(d)) return;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
