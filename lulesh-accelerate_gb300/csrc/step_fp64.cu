@@ -23,7 +23,6 @@
 // order and the constraint minima use an order-independent integer min.
 #include "lulesh_internal.h"
 #include "kernels.h"
-#include "geometry.cuh"
 #include "hexmodes.cuh"
 #include "common.cuh"
 #include "batch_kernels.cuh"

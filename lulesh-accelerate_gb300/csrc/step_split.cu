@@ -24,7 +24,6 @@
 // Launch structure and error handling are those of step_fp64.cu.
 #include "lulesh_internal.h"
 #include "kernels.h"
-#include "geometry.cuh"
 #include "hexmodes.cuh"
 #include "common.cuh"
 #include "batch_kernels.cuh"
@@ -209,65 +208,72 @@ __device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars
 
     int nl[8];
     load_nodelist(d.nodelist, k, nl);
-    float x[8], y[8], z[8];
-    rel8(d.xs, nl, x);
-    rel8(d.ys, nl, y);
-    rel8(d.zs, nl, z);
-
-    float f[3][8];
+    // The geometry of the FP64 kernel (the Walsh-mode identities of
+    // hexmodes.cuh) in FP32, on corner coordinates relative to corner 0: the
+    // modes M1..M7 do not see a translation.
+    V3<float> M[7];
     {
-        const float determ = jacobian_volume<float>(x, y, z);
-        if (determ <= 0.f) flag_error(sc, ERR_K1_DETERM, k);
-        float pf[3][8];
-        node_normals_diag<float>(pf, x, y, z);
-        const float sig = -d2f(d.p[k]) - d2f(d.q[k]);
+        float x[8], y[8], z[8], mx[7], my[7], mz[7];
+        rel8(d.xs, nl, x);
+        rel8(d.ys, nl, y);
+        rel8(d.zs, nl, z);
+        walsh8(x, mx);
+        walsh8(y, my);
+        walsh8(z, mz);
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            f[0][c] = -(sig * pf[0][c]);
-            f[1][c] = -(sig * pf[1][c]);
-            f[2][c] = -(sig * pf[2][c]);
-        }
+        for (int i = 0; i < 7; ++i) M[i] = mode(mx, my, mz, i);
+    }
+    float dvdx[8], dvdy[8], dvdz[8];
+    V3<float> nx[3];
+    force_geometry(M[0], M[1], M[2], M[3], M[4], M[5], dvdx, dvdy, dvdz, nx);   // 192 x dV/dx, normal generators
+
+    // IntegrateStressForElems (LULESH-OMP.cc:853-903): the stress force of
+    // the corner with signs s is s . (Y1, Y2, Y3) with Y = ((p + q)/64) X;
+    // corners 4..7 carry the forces of corners 2, 3, 0, 1 negated.  Only the
+    // sign of the Jacobian volume M2.(M3 x M1) / 64 is tested.
+    if (dot3(M[1], cross3(M[2], M[0])) <= 0.f) flag_error(sc, ERR_K1_DETERM, k);
+    const float w = (1.f / 64.f) * (d2f(d.p[k]) + d2f(d.q[k]));
+    float f[3][8];
+#pragma unroll
+    for (int dim = 0; dim < 3; ++dim) {
+        const float y1 = w * (dim == 0 ? nx[0].x : dim == 1 ? nx[0].y : nx[0].z);
+        const float y2 = w * (dim == 0 ? nx[1].x : dim == 1 ? nx[1].y : nx[1].z);
+        const float y3 = w * (dim == 0 ? nx[2].x : dim == 1 ? nx[2].y : nx[2].z);
+        const float a = y1 + y2, b = y1 - y2;
+        f[dim][0] = -(a + y3);   // (-,-,-)
+        f[dim][1] = b - y3;      // (+,-,-)
+        f[dim][2] = a - y3;      // (+,+,-)
+        f[dim][3] = -(b + y3);   // (-,+,-)
+        f[dim][4] = -f[dim][2];
+        f[dim][5] = -f[dim][3];
+        f[dim][6] = -f[dim][0];
+        f[dim][7] = -f[dim][1];
     }
 
     const double vk = d.v[k];
     if (vk <= 0.0) flag_error(sc, ERR_K1_VOLUME, k);
     const float hourg = d2f(d.prm.hgcoef);
     if (hourg > 0.f) {
-        const float determ = d2f(d.volo[k]) * d2f(vk);
+        // CalcFBHourglassForceForElems (:1291-1473): hourgam = gamma -
+        // volinv (dV/dx . hourmod), the hourglass projections being the
+        // modes M6, M5, M4, M7
+        const float r = rcbrtf(d2f(d.volo[k]) * d2f(vk));      // determ^(-1/3)
+        const float volinv192 = ((r * r) * r) * (1.f / 192.f);
+        const V3<float> H[4] = {M[5], M[4], M[3], M[6]};
+        const float gam[4][8] = {
+            { 1.f,  1.f, -1.f, -1.f, -1.f, -1.f,  1.f,  1.f},
+            { 1.f, -1.f, -1.f,  1.f, -1.f,  1.f,  1.f, -1.f},
+            { 1.f, -1.f,  1.f, -1.f,  1.f, -1.f,  1.f, -1.f},
+            {-1.f,  1.f, -1.f,  1.f,  1.f, -1.f,  1.f, -1.f}};
         float hg[8][4];
-        {
-            float dvdx[8], dvdy[8], dvdz[8];
-            volume_derivative<float>(dvdx, dvdy, dvdz, x, y, z);
-            const float volinv = 1.f / determ;
-#define HMOD(f, s0, s1, s2, s3, s4, s5, s6, s7) \
-            ((((((((s0 f[0]) s1 f[1]) s2 f[2]) s3 f[3]) s4 f[4]) s5 f[5]) s6 f[6]) s7 f[7])
-            float hx[4], hy[4], hz[4];
-            hx[0] = HMOD(x, +, +, -, -, -, -, +, +);
-            hy[0] = HMOD(y, +, +, -, -, -, -, +, +);
-            hz[0] = HMOD(z, +, +, -, -, -, -, +, +);
-            hx[1] = HMOD(x, +, -, -, +, -, +, +, -);
-            hy[1] = HMOD(y, +, -, -, +, -, +, +, -);
-            hz[1] = HMOD(z, +, -, -, +, -, +, +, -);
-            hx[2] = HMOD(x, +, -, +, -, +, -, +, -);
-            hy[2] = HMOD(y, +, -, +, -, +, -, +, -);
-            hz[2] = HMOD(z, +, -, +, -, +, -, +, -);
-            hx[3] = HMOD(x, -, +, -, +, +, -, +, -);
-            hy[3] = HMOD(y, -, +, -, +, +, -, +, -);
-            hz[3] = HMOD(z, -, +, -, +, +, -, +, -);
-#undef HMOD
-            const float gam[4][8] = {
-                { 1.f,  1.f, -1.f, -1.f, -1.f, -1.f,  1.f,  1.f},
-                { 1.f, -1.f, -1.f,  1.f, -1.f,  1.f,  1.f, -1.f},
-                { 1.f, -1.f,  1.f, -1.f,  1.f, -1.f,  1.f, -1.f},
-                {-1.f,  1.f, -1.f,  1.f,  1.f, -1.f,  1.f, -1.f}};
 #pragma unroll
-            for (int m = 0; m < 4; ++m)
+        for (int m = 0; m < 4; ++m) {
+            const float hx = -(volinv192 * H[m].x), hy = -(volinv192 * H[m].y), hz = -(volinv192 * H[m].z);
 #pragma unroll
-                for (int c = 0; c < 8; ++c)
-                    hg[c][m] = gam[m][c] - volinv * (dvdx[c] * hx[m] + dvdy[c] * hy[m] + dvdz[c] * hz[m]);
+            for (int c = 0; c < 8; ++c)
+                hg[c][m] = fmaf(dvdz[c], hz, fmaf(dvdy[c], hy, fmaf(dvdx[c], hx, gam[m][c])));
         }
-        const float coefficient =
-            (((-hourg) * 0.01f) * d2f(d.ss[k])) * d2f(d.elem_mass[k]) / cbrtf(determ);
+        const float coefficient = (((-hourg) * 0.01f) * d2f(d.ss[k])) * d2f(d.elem_mass[k]) * r;
         // velocities relative to corner 0: the hourglass modes are blind to
         // a uniform velocity (sum over corners of each hourgam column is 0)
         const float2 *vel[3] = {d.xds, d.yds, d.zds};
@@ -280,12 +286,12 @@ __device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars
             for (int m = 0; m < 4; ++m) {
                 float acc = hg[1][m] * u[1];
 #pragma unroll
-                for (int c = 2; c < 8; ++c) acc = acc + hg[c][m] * u[c];
-                h[m] = acc;
+                for (int c = 2; c < 8; ++c) acc = fmaf(hg[c][m], u[c], acc);
+                h[m] = coefficient * acc;
             }
 #pragma unroll
             for (int c = 0; c < 8; ++c)
-                f[dim][c] += coefficient * (((hg[c][0] * h[0] + hg[c][1] * h[1]) + hg[c][2] * h[2]) + hg[c][3] * h[3]);
+                f[dim][c] = fmaf(hg[c][3], h[3], fmaf(hg[c][2], h[2], fmaf(hg[c][1], h[1], fmaf(hg[c][0], h[0], f[dim][c]))));
         }
     }
 #pragma unroll
