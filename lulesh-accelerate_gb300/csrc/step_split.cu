@@ -303,9 +303,9 @@ __device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars
 }
 
 // The FP32 force kernel waits on its corner gathers rather than on an
-// arithmetic pipe, so it is held to 96 registers (five 128-thread blocks per
-// SM instead of four; 8 bytes spilled): 0.52 -> 0.48 ms at s=192.
-__global__ void __launch_bounds__(kBlockElem, 5) k_elem_force_split(const __grid_constant__ Dom d)
+// arithmetic pipe, so it is held to 64 registers (eight 128-thread blocks
+// per SM instead of four; ~200 bytes spilled): 0.48 -> 0.43 ms at s=192.
+__global__ void __launch_bounds__(kBlockElem, 8) k_elem_force_split(const __grid_constant__ Dom d)
 {
     if (skip_step(d)) return;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -431,11 +431,11 @@ __device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevSc
     gq[1 * ne + k] = vscale * dot3(Cf.c31, V[1].hi);                                 // delv_eta
 }
 
-// Held to 96 registers (five blocks per SM; a few hundred bytes spilled):
+// Held to 80 registers (six blocks per SM; a few hundred bytes spilled):
 // with its FP64 work cut by the first-order corrections the kernel waits on
-// its corner gathers, and the extra resident block pays (1.27 -> 1.16 ms at
-// s=192 against the unbounded 128 registers).
-__global__ void __launch_bounds__(kBlockElem, 5) k_elem_kinematics_split(const __grid_constant__ Dom d)
+// its corner gathers, and the extra resident blocks pay (1.27 -> 1.15 ms at
+// s=192 against the unbounded 128 registers; eight blocks spill too much).
+__global__ void __launch_bounds__(kBlockElem, 6) k_elem_kinematics_split(const __grid_constant__ Dom d)
 {
     if (skip_step(d)) return;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
