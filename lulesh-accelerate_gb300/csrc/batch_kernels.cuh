@@ -11,7 +11,7 @@
 namespace lulesh {
 
 template <void (*Body)(const Dom &, int, DevScalars *)>
-__global__ void kb_elem(const __grid_constant__ Dom d, const __grid_constant__ BatchView b, int cls)
+__device__ __forceinline__ void kb_elem_tiles(const Dom &d, const BatchView &b, int cls)
 {
     const int n_act = b.counts[cls];
     const int *list = b.active_etiles + b.eclass_off[cls];
@@ -25,26 +25,11 @@ __global__ void kb_elem(const __grid_constant__ Dom d, const __grid_constant__ B
     }
 }
 
-template <void (*Body)(const Dom &, int, const DevScalars *)>
-__global__ void kb_node(const __grid_constant__ Dom d, const __grid_constant__ BatchView b, int cls)
-{
-    const int n_act = b.counts[kMaxClasses + cls];
-    const int *list = b.active_ntiles + b.nclass_off[cls];
-    for (int i = blockIdx.x; i < n_act; i += gridDim.x) {
-        const int t = list[i];
-        const int inst = b.ntile_inst[t];
-        const DevScalars *sc = d.sc + inst;
-        if (sc->err_any) continue;
-        const int end = min(b.inst_node_end[inst], (t + 1) * kTile);
-        for (int n = t * kTile + threadIdx.x; n < end; n += blockDim.x) Body(d, n, sc);
-    }
-}
-
 // The material kernel also reduces the instance's constraint keys: one
 // block minimum per tile (every thread reaches the barrier; the trip counts
 // are uniform over the block).
 template <void (*Body)(const Dom &, int, DevScalars *, unsigned long long &, unsigned long long &)>
-__global__ void kb_material(const __grid_constant__ Dom d, const __grid_constant__ BatchView b, int cls)
+__device__ __forceinline__ void kb_material_tiles(const Dom &d, const BatchView &b, int cls)
 {
     const int n_act = b.counts[cls];
     const int *list = b.active_etiles + b.eclass_off[cls];
@@ -64,6 +49,57 @@ __global__ void kb_material(const __grid_constant__ Dom d, const __grid_constant
         }
         block_min_publish(kc, kh, sc);
         __syncthreads();   // the shared staging of block_min_publish is reused next tile
+    }
+}
+
+template <void (*Body)(const Dom &, int, DevScalars *)>
+__global__ void kb_elem(const __grid_constant__ Dom d, const __grid_constant__ BatchView b, int cls)
+{
+    kb_elem_tiles<Body>(d, b, cls);
+}
+
+template <void (*Body)(const Dom &, int, DevScalars *, unsigned long long &, unsigned long long &)>
+__global__ void kb_material(const __grid_constant__ Dom d, const __grid_constant__ BatchView b, int cls)
+{
+    kb_material_tiles<Body>(d, b, cls);
+}
+
+// Register-capped variants for the split-precision kinematics and material
+// bodies, which wait on their gathers: blocks of up to kBatchMaxBlock
+// threads (the autotuner's largest), kMinBlocks of them resident per SM, so
+// 4 -> 64 registers and 2 -> 128.  On the 528-instance split ensemble
+// (kinematics at 128 registers instead of 134, material at 64 instead of 77)
+// this took 36.7 s to 30.2 s; capping the force body as well (64 or 85
+// registers, with spills) lost 5 %.
+constexpr int kBatchMaxBlock = 256;
+
+template <void (*Body)(const Dom &, int, DevScalars *), int kMinBlocks>
+__global__ void __launch_bounds__(kBatchMaxBlock, kMinBlocks)
+    kb_elem_capped(const __grid_constant__ Dom d, const __grid_constant__ BatchView b, int cls)
+{
+    kb_elem_tiles<Body>(d, b, cls);
+}
+
+template <void (*Body)(const Dom &, int, DevScalars *, unsigned long long &, unsigned long long &),
+          int kMinBlocks>
+__global__ void __launch_bounds__(kBatchMaxBlock, kMinBlocks)
+    kb_material_capped(const __grid_constant__ Dom d, const __grid_constant__ BatchView b, int cls)
+{
+    kb_material_tiles<Body>(d, b, cls);
+}
+
+template <void (*Body)(const Dom &, int, const DevScalars *)>
+__global__ void kb_node(const __grid_constant__ Dom d, const __grid_constant__ BatchView b, int cls)
+{
+    const int n_act = b.counts[kMaxClasses + cls];
+    const int *list = b.active_ntiles + b.nclass_off[cls];
+    for (int i = blockIdx.x; i < n_act; i += gridDim.x) {
+        const int t = list[i];
+        const int inst = b.ntile_inst[t];
+        const DevScalars *sc = d.sc + inst;
+        if (sc->err_any) continue;
+        const int end = min(b.inst_node_end[inst], (t + 1) * kTile);
+        for (int n = t * kTile + threadIdx.x; n < end; n += blockDim.x) Body(d, n, sc);
     }
 }
 

@@ -566,8 +566,8 @@ void launch_batch_kernel_split(const Dom &d, const BatchView &b, cudaStream_t st
     switch (kernel) {
     case 0: kb_elem<elem_force_split><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     case 1: kb_node<node_update_split><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
-    case 2: kb_elem<elem_kinematics_split><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
-    default: kb_material<elem_material_split<true>><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    case 2: kb_elem_capped<elem_kinematics_split, 2><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    default: kb_material_capped<elem_material_split<true>, 4><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     }
 }
 
@@ -579,8 +579,8 @@ int batch_max_blocks_split(int kernel, int block)
     switch (kernel) {
     case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_force_split>, block, 0); break;
     case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_node<node_update_split>, block, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_kinematics_split>, block, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material<elem_material_split<true>>, block, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem_capped<elem_kinematics_split, 2>, block, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material_capped<elem_material_split<true>, 4>, block, 0); break;
     }
     return e == cudaSuccess ? n : 0;
 }
