@@ -56,6 +56,24 @@ def test_split_full_run_s30(pkg, answers):
     assert mr <= 1e-5, mr
 
 
+def test_split_small_ensemble_instances(pkg):
+    """The seeded 528-instance ensemble's most sensitive small instances
+    (s = 13..26, energy factors 0.57..1.78), run to t = 1e-2 as a split and
+    an FP64 batch: origin energies within the split bar of each other.  An
+    approximate FP32 reciprocal root in the characteristic length once moved
+    these to 2.2e-6 while the s=30 and s=192 checks stayed green."""
+    sizes, scale = [21, 13, 13, 26, 27, 40], [0.568, 1.704, 1.488, 1.778, 0.514, 1.175]
+    e0 = {}
+    for name, prec in (("fp64", pkg.FP64), ("split", pkg.SPLIT)):
+        with pkg.Batch(sizes, scale, pkg.INIT_V2, prec) as b:
+            b.run()
+            e0[name] = [(b.instance(i)[1], b.instance(i)[0].cycle) for i in range(len(sizes))]
+    for i, s in enumerate(sizes):
+        (ef, cf), (es, cs) = e0["fp64"][i], e0["split"][i]
+        assert cs == cf, (s, cs, cf)
+        assert abs(es - ef) / abs(ef) <= E0_TOL, (s, scale[i], abs(es - ef) / abs(ef))
+
+
 def test_split_tracks_fp64_at_s192(pkg):
     """s=192, 100 cycles: the four reported results of the split path against
     the plain FP64 path on the same GPU."""
