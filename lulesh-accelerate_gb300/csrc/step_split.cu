@@ -15,11 +15,13 @@
 //
 // Corner forces are FP32 and summed per node with a compensated (Kahan)
 // FP32 sum whose two words are combined in FP64.  FP32 geometry never sees an
-// absolute coordinate: every element works on its corners relative to corner
-// 0, formed from a hi/lo float pair that the node kernel keeps beside each
-// FP64 position and velocity ((hi_c - hi_0) + (lo_c - lo_0) carries the
-// difference to ~2^-48 of the coordinate), so FP32 round-off is relative to
-// the element size, not to the mesh extent.
+// absolute coordinate: the force kernel works on the corners relative to
+// corner 0, formed from a hi/lo float pair that the node kernel keeps beside
+// each FP64 position and velocity ((hi_c - hi_0) + (lo_c - lo_0) carries the
+// difference to ~2^-48 of the coordinate), and the kinematics kernel on the
+// Walsh modes of the corners (differences only), summed exactly from the
+// same pairs; so FP32 round-off is relative to the element size, not to the
+// mesh extent.
 //
 // Launch structure and error handling are those of step_fp64.cu.
 #include "lulesh_internal.h"
