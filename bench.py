@@ -346,7 +346,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
     ap.add_argument("--profile-cycles", type=int, default=20)
     ap.add_argument("--e2e-cycles", type=int, default=0, help="0: same as --steps")
-    ap.add_argument("--cpu-cycles", type=int, default=8, help="cycles of the CPU baseline sample")
+    ap.add_argument("--cpu-cycles", type=int, default=40,
+                    help="cycles of the CPU baseline sample (about 10 s of the 16-core host at s=192)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-split", action="store_true", help="skip the split-precision leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble legs")
