@@ -158,6 +158,7 @@ int clear_errors(lulesh_ctx *ctx)
     CK(cudaStreamSynchronize(ctx->stream));
     h->err_any = 0;
     for (int i = 0; i < ERR_NUM; ++i) h->err[i] = 0;
+    h->geo_valid = 0;   // the host may have replaced positions
     CK(cudaMemcpyAsync(ctx->dom.sc, h, sizeof(DevScalars), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->status = LULESH_OK;
@@ -361,6 +362,7 @@ int create_from_mesh(const HostMesh &m, int precision, const lulesh_params *para
     A(d.delx_xi, ne); A(d.delx_eta, ne); A(d.delx_zeta, ne);
     if (precision == LULESH_PRECISION_FP64) {
         A(d.fcx, 8 * ne); A(d.fcy, 8 * ne); A(d.fcz, 8 * ne);
+        A(d.geo, (size_t)kGeoWords * ne);
     } else {
         A(d.f32x, 8 * ne); A(d.f32y, 8 * ne); A(d.f32z, 8 * ne);
         A(d.xs, nn); A(d.ys, nn); A(d.zs, nn); A(d.xds, nn); A(d.yds, nn); A(d.zds, nn);
@@ -621,6 +623,7 @@ int lulesh_upload_domain(lulesh_ctx *ctx, const double *x, const double *y, cons
     ctx->h_sc->deltatime = deltatime;
     ctx->h_sc->err_any = 0;
     for (int i = 0; i < ERR_NUM; ++i) ctx->h_sc->err[i] = 0;
+    ctx->h_sc->geo_valid = 0;   // new positions: the geometry cache is stale
     CK(cudaMemcpyAsync(d.sc, ctx->h_sc, sizeof(DevScalars), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->status = LULESH_OK;

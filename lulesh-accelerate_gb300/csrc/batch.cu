@@ -119,6 +119,12 @@ long round_tile(long n) { return (n + kTile - 1) / kTile * kTile; }
 
 // ---- control kernels ---------------------------------------------------
 
+__global__ void kb_geo_invalidate(DevScalars *sc, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) sc[i].geo_valid = 0;
+}
+
 __global__ void kb_time_increment(const __grid_constant__ Dom d, const __grid_constant__ BatchView b)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -513,6 +519,7 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
     A(d.delx_xi, ne); A(d.delx_eta, ne); A(d.delx_zeta, ne);
     if (precision == LULESH_PRECISION_FP64) {
         A(d.fcx, 8 * ne); A(d.fcy, 8 * ne); A(d.fcz, 8 * ne);
+        A(d.geo, (size_t)kGeoWords * ne);
     } else {
         A(d.f32x, 8 * ne); A(d.f32y, 8 * ne); A(d.f32z, 8 * ne);
         A(d.xs, nn); A(d.ys, nn); A(d.zs, nn); A(d.xds, nn); A(d.yds, nn); A(d.zds, nn);
@@ -601,6 +608,8 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
         h.dthydro = 1.0e+20;
         h.courant_key = ~0ULL;
         h.hydro_key = ~0ULL;
+        h.elem_begin = (int)eo_i;
+        h.node_begin = (int)no_i;
         iee_h[i] = (int)(eo_i + nei);
         ine_h[i] = (int)(no_i + nni);
         cpos += 8 * nei;
@@ -845,6 +854,9 @@ int lulesh_batch_autotune(lulesh_batch *b, const char *cache_path, int retune)
             cudaMemcpyAsync(j < 6 ? node_f[j] : elem_f[j - 6], snap[j], (j < 6 ? nn : ne) * sizeof(double),
                             cudaMemcpyDeviceToDevice, b->stream);
         cudaMemcpyAsync(d.sc, ssnap, sizeof(DevScalars) * b->n, cudaMemcpyDeviceToDevice, b->stream);
+        // the tuning runs rewrote the geometry cache from positions that are
+        // now restored: mark it stale
+        kb_geo_invalidate<<<(b->n + 127) / 128, 128, 0, b->stream>>>(d.sc, b->n);
         if (b->precision == LULESH_PRECISION_SPLIT) launch_split_sync(b->dom, b->stream);
         cudaError_t e = cudaStreamSynchronize(b->stream);
         cleanup();

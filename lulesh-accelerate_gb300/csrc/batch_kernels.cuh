@@ -98,6 +98,8 @@ __global__ void kb_node(const __grid_constant__ Dom d, const __grid_constant__ B
         const int inst = b.ntile_inst[t];
         const DevScalars *sc = d.sc + inst;
         if (sc->err_any) continue;
+        // the instance's positions move: its geometry cache goes stale
+        if (d.geo && threadIdx.x == 0) d.sc[inst].geo_valid = 0;
         const int end = min(b.inst_node_end[inst], (t + 1) * kTile);
         for (int n = t * kTile + threadIdx.x; n < end; n += blockDim.x) Body(d, n, sc);
     }

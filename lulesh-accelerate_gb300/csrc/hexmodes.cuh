@@ -130,8 +130,24 @@ __device__ __forceinline__ void inv_walsh6(T q1, T q2, T q3, T q4, T q5, T q6, T
     v[7] = emp + fmp;
 }
 
+// The six cross products of the modes that the volume, the node normals, the
+// Q gradients and the face areas share: c23 = M2xM3, c31 = M3xM1, c12 = M1xM2,
+// c45 = M4xM5, c64 = M6xM4, c56 = M5xM6.
+template <typename T>
+struct ModeCrosses {
+    V3<T> c23, c31, c12, c45, c64, c56;
+};
+
+template <typename T>
+__device__ __forceinline__ ModeCrosses<T> mode_crosses(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
+                                                       const V3<T> &M4, const V3<T> &M5, const V3<T> &M6)
+{
+    return {cross3(M2, M3), cross3(M3, M1), cross3(M1, M2), cross3(M4, M5), cross3(M6, M4), cross3(M5, M6)};
+}
+
 // 192 x the volume derivative of each corner (dx/dy/dz[c] = 192 dV/dx_c)
-// and the three vectors nx[0..2] = X1, X2, X3 that give the node normals.
+// and the three vectors nx[0..2] = X1, X2, X3 that give the node normals,
+// from the modes and their shared cross products C.
 // The node normals, sums of the quarter-area vectors of each corner's three
 // faces (CalcElemNodeNormals :708-799), are linear in the corner's signs:
 // pf[c] = (s_xi X1 + s_eta X2 + s_zeta X3)/64 with X1 = M2xM3 + M4xM5,
@@ -143,11 +159,9 @@ __device__ __forceinline__ void inv_walsh6(T q1, T q2, T q3, T q4, T q5, T q6, T
 template <typename T>
 __device__ __forceinline__ void force_geometry(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
                                                const V3<T> &M4, const V3<T> &M5, const V3<T> &M6,
-                                               T dx[8], T dy[8], T dz[8], V3<T> nx[3])
+                                               const ModeCrosses<T> &C, T dx[8], T dy[8], T dz[8], V3<T> nx[3])
 {
-    const V3<T> c23 = cross3(M2, M3), c45 = cross3(M4, M5);
-    const V3<T> c31 = cross3(M3, M1), c64 = cross3(M6, M4);
-    const V3<T> c12 = cross3(M1, M2), c56 = cross3(M5, M6);
+    const V3<T> &c23 = C.c23, &c45 = C.c45, &c31 = C.c31, &c64 = C.c64, &c12 = C.c12, &c56 = C.c56;
     auto add3 = [](const V3<T> &a, T s, const V3<T> &b) {
         return V3<T>{a.x * s + b.x, a.y * s + b.y, a.z * s + b.z};
     };
@@ -165,21 +179,6 @@ __device__ __forceinline__ void force_geometry(const V3<T> &M1, const V3<T> &M2,
     nx[0] = sum3(c23, c45);
     nx[1] = sum3(c31, c64);
     nx[2] = sum3(c12, c56);
-}
-
-// The six cross products of the modes that the volume, the node normals, the
-// Q gradients and the face areas share: c23 = M2xM3, c31 = M3xM1, c12 = M1xM2,
-// c45 = M4xM5, c64 = M6xM4, c56 = M5xM6.
-template <typename T>
-struct ModeCrosses {
-    V3<T> c23, c31, c12, c45, c64, c56;
-};
-
-template <typename T>
-__device__ __forceinline__ ModeCrosses<T> mode_crosses(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
-                                                       const V3<T> &M4, const V3<T> &M5, const V3<T> &M6)
-{
-    return {cross3(M2, M3), cross3(M3, M1), cross3(M1, M2), cross3(M4, M5), cross3(M6, M4), cross3(M5, M6)};
 }
 
 // 64 x volume through the shared crosses: the bilinear terms of the volume formula above are

@@ -43,7 +43,8 @@ struct DevScalars {
     int err[ERR_NUM];                    // first offending element + 1, 0 = none
     int run_cycles;                      // cycles done by the current lulesh_run
     int run_max;                         // its cap (<= 0: none)
-    int pad;
+    int geo_valid;                       // Dom::geo holds the current positions' geometry
+    int elem_begin, node_begin;          // first element / node of the instance (batches)
     unsigned long long courant_key;      // order-preserving keys of the
     unsigned long long hydro_key;        // constraint minima (see keys below)
 };
@@ -88,6 +89,9 @@ void set_last_error(const std::string &msg);
 void default_params(lulesh_params *p);
 
 // Everything one kernel launch needs, passed by value.
+// Words per element of the FP64 path's geometry cache (Dom::geo).
+constexpr int kGeoWords = 39;
+
 struct Dom {
     int s, ne, nn;
     int keep;                            // bit0: store nodal forces, bit1: store ql/qq
@@ -125,6 +129,12 @@ struct Dom {
     float2 *xs, *ys, *zs, *xds, *yds, *zds;
     double *inv_mass;
     double *inv_volo;                    // [ne] 1/volo (the element kernels need it)
+    // FP64 path: element geometry of the current positions, left by the
+    // kinematics kernel for the next cycle's force kernel (the positions do
+    // not change between the two): the Walsh modes M1..M7 (21 words) and the
+    // six shared cross products (18 words), [kGeoWords][ne]; valid while
+    // DevScalars::geo_valid is set.  Null: not kept.
+    double *geo;
     float *gq;
     DevScalars *sc;
     const int *gate;                     // host-driven run loop: cycle runs while *gate != 0

@@ -41,6 +41,44 @@ __global__ void k_time_increment(const __grid_constant__ Dom d)
 }
 
 // ---------------------------------------------------------------------
+// Geometry cache (Dom::geo): modes M1..M7 of x, y, z, then the six shared
+// cross products, one word per element per plane
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void store_geometry(double *__restrict__ g, size_t ne, int k, const double mx[7],
+                                               const double my[7], const double mz[7], const ModeCrosses<double> &X)
+{
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        g[(3 * i + 0) * ne + k] = mx[i];
+        g[(3 * i + 1) * ne + k] = my[i];
+        g[(3 * i + 2) * ne + k] = mz[i];
+    }
+    const V3<double> c[6] = {X.c23, X.c31, X.c12, X.c45, X.c64, X.c56};
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        g[(21 + 3 * i) * ne + k] = c[i].x;
+        g[(22 + 3 * i) * ne + k] = c[i].y;
+        g[(23 + 3 * i) * ne + k] = c[i].z;
+    }
+}
+
+__device__ __forceinline__ void load_geometry(const double *__restrict__ g, size_t ne, int k, double mx[7],
+                                              double my[7], double mz[7], ModeCrosses<double> &X)
+{
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        mx[i] = __ldg(g + (3 * i + 0) * ne + k);
+        my[i] = __ldg(g + (3 * i + 1) * ne + k);
+        mz[i] = __ldg(g + (3 * i + 2) * ne + k);
+    }
+    V3<double> c[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        c[i] = {__ldg(g + (21 + 3 * i) * ne + k), __ldg(g + (22 + 3 * i) * ne + k), __ldg(g + (23 + 3 * i) * ne + k)};
+    X = {c[0], c[1], c[2], c[3], c[4], c[5]};
+}
+
+// ---------------------------------------------------------------------
 // Element force: stress + Flanagan-Belytschko hourglass
 // ---------------------------------------------------------------------
 __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars *sc)
@@ -48,20 +86,31 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
     const size_t ne = (size_t)d.ne;
     int nl[8];
     load_nodelist(d.nodelist, k, nl);
-    double x[8], y[8], z[8];
-    gather8(d.x, nl, x);
-    gather8(d.y, nl, y);
-    gather8(d.z, nl, z);
+    // The Walsh modes of the corner coordinates and their shared cross
+    // products: left by the previous cycle's kinematics kernel for these
+    // same positions when it kept them (the same functions of the same
+    // values, so the same bits), else formed here.  The node update that
+    // follows moves the positions and clears the mark.
     double mx[7], my[7], mz[7];
-    walsh8(x, mx);
-    walsh8(y, my);
-    walsh8(z, mz);
+    ModeCrosses<double> X;
+    if (d.geo && sc->geo_valid) {
+        load_geometry(d.geo, ne, k, mx, my, mz, X);
+    } else {
+        double x[8], y[8], z[8];
+        gather8(d.x, nl, x);
+        gather8(d.y, nl, y);
+        gather8(d.z, nl, z);
+        walsh8(x, mx);
+        walsh8(y, my);
+        walsh8(z, mz);
+        X = mode_crosses(mode(mx, my, mz, 0), mode(mx, my, mz, 1), mode(mx, my, mz, 2), mode(mx, my, mz, 3),
+                         mode(mx, my, mz, 4), mode(mx, my, mz, 5));
+    }
     const V3<double> M1 = mode(mx, my, mz, 0), M2 = mode(mx, my, mz, 1), M3 = mode(mx, my, mz, 2);
-
     const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
     double dvdx[8], dvdy[8], dvdz[8];
     V3<double> nx[3];
-    force_geometry(M1, M2, M3, M4, M5, M6, dvdx, dvdy, dvdz, nx);   // 192 x dV/dx, normal generators
+    force_geometry(M1, M2, M3, M4, M5, M6, X, dvdx, dvdy, dvdz, nx);   // 192 x dV/dx, normal generators
 
     // IntegrateStressForElems (LULESH-OMP.cc:853-903): sig = -p - q and the
     // corner force -sig * (area-weighted node normal).  The normal of the
@@ -79,7 +128,7 @@ __device__ __forceinline__ void elem_force_fp64(const Dom &d, int k, DevScalars 
             Y[i][1] = w * nx[i].y;
             Y[i][2] = w * nx[i].z;
         }
-        const double determ64 = dot3(M2, cross3(M3, M1));
+        const double determ64 = dot3(M2, X.c31);
         if (determ64 <= 0.0) flag_error(sc, ERR_K1_DETERM, k);
     }
     // stress force of corners 0..3 in one component (corners 4..7: 2, 3,
@@ -229,6 +278,7 @@ __global__ void __launch_bounds__(kBlockNode) k_node_update(const __grid_constan
     if (skip_step(d)) return;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= d.nn) return;
+    if (n == 0 && d.geo) d.sc->geo_valid = 0;   // the positions move: the geometry cache goes stale
     node_update_fp64(d, n, d.sc);
 }
 
@@ -263,6 +313,11 @@ __device__ __forceinline__ void elem_kinematics_fp64(const Dom &d, int k, DevSca
     // CalcKinematicsForElems, volume part (:1950-1964)
     const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
     const ModeCrosses<double> X = mode_crosses(M1, M2, M3, M4, M5, M6);
+    if (d.geo) {
+        // the next cycle's force kernel works on these same positions
+        store_geometry(d.geo, (size_t)d.ne, k, mx, my, mz, X);
+        if (k == sc->elem_begin) sc->geo_valid = 1;
+    }
     const double volo = d.volo[k];
     const double vol64 = volume64_shared(M1, M2, M3, X);
     const double volume = vol64 * (1.0 / 64.0);

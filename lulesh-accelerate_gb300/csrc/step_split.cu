@@ -227,13 +227,14 @@ __device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars
     }
     float dvdx[8], dvdy[8], dvdz[8];
     V3<float> nx[3];
-    force_geometry(M[0], M[1], M[2], M[3], M[4], M[5], dvdx, dvdy, dvdz, nx);   // 192 x dV/dx, normal generators
+    const ModeCrosses<float> C = mode_crosses(M[0], M[1], M[2], M[3], M[4], M[5]);
+    force_geometry(M[0], M[1], M[2], M[3], M[4], M[5], C, dvdx, dvdy, dvdz, nx);   // 192 x dV/dx, normal generators
 
     // IntegrateStressForElems (LULESH-OMP.cc:853-903): the stress force of
     // the corner with signs s is s . (Y1, Y2, Y3) with Y = ((p + q)/64) X;
     // corners 4..7 carry the forces of corners 2, 3, 0, 1 negated.  Only the
     // sign of the Jacobian volume M2.(M3 x M1) / 64 is tested.
-    if (dot3(M[1], cross3(M[2], M[0])) <= 0.f) flag_error(sc, ERR_K1_DETERM, k);
+    if (dot3(M[1], C.c31) <= 0.f) flag_error(sc, ERR_K1_DETERM, k);
     const float w = (1.f / 64.f) * (d2f(d.p[k]) + d2f(d.q[k]));
     float f[3][8];
 #pragma unroll
