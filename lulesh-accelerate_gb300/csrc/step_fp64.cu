@@ -313,11 +313,12 @@ __device__ __forceinline__ void elem_kinematics_fp64(const Dom &d, int k, DevSca
     // CalcKinematicsForElems, volume part (:1950-1964)
     const V3<double> M4 = mode(mx, my, mz, 3), M5 = mode(mx, my, mz, 4), M6 = mode(mx, my, mz, 5);
     const ModeCrosses<double> X = mode_crosses(M1, M2, M3, M4, M5, M6);
-    if (d.geo) {
-        // the next cycle's force kernel works on these same positions
-        store_geometry(d.geo, (size_t)d.ne, k, mx, my, mz, X);
-        if (k == sc->elem_begin) sc->geo_valid = 1;
-    }
+    // The next cycle's force kernel works on these same positions.  Every
+    // context that runs this kernel keeps the cache (only the nodal-only
+    // entry point has none), and the store is unconditional: behind a branch
+    // the compiler formed the cross products twice (36 more FP64 operations).
+    store_geometry(d.geo, (size_t)d.ne, k, mx, my, mz, X);
+    if (k == sc->elem_begin) sc->geo_valid = 1;
     const double volo = d.volo[k];
     const double vol64 = volume64_shared(M1, M2, M3, X);
     const double volume = vol64 * (1.0 / 64.0);
