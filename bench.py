@@ -73,15 +73,16 @@ def algorithmic_bytes(ne: int, nn: int, precision: str = "fp64") -> dict:
         }
     return {
         "time_increment": 0,
-        # x,y,z,xd,yd,zd gathered (48/node), nodelist (32), p q v volo ss mass
-        # (48) in; corner forces (24 doubles, stress plus hourglass) out
-        "elem_force": 48 * nn + (32 + 48 + 192) * ne,
+        # xd,yd,zd gathered (24/node), nodelist (32), the geometry cache the
+        # kinematics kernel left (39 doubles), p q v volo ss mass (48) in;
+        # corner forces (24 doubles, stress plus hourglass) out
+        "elem_force": 24 * nn + (32 + 312 + 48 + 192) * ne,
         # corner slots (32/elem) + start (4/node), corner forces (192/elem),
         # 1/mass (8) + bc (1), x..zd read and written (96)
         "node_update": (4 + 8 + 1 + 96) * nn + (32 + 192) * ne,
         # nodelist, x..zd gathered, volo, 1/volo, v in; vnew delv arealg vdov
-        # delv_* delx_* out
-        "elem_kinematics": 48 * nn + (32 + 24 + 80) * ne,
+        # delv_* delx_* and the geometry cache (39 doubles) out
+        "elem_kinematics": 48 * nn + (32 + 24 + 80 + 312) * ne,
         # bc + 6 neighbour ids, delv_* delx_*, vnew volo vdov delv mass q v e p
         # arealg in; p e q ss v out
         "elem_material": (4 + 24 + 48 + 80 + 40) * ne,
@@ -315,7 +316,7 @@ def config_for(args, ne, nn) -> dict:
     return {"workload": f"sedov_s{args.size}_{args.precision}", "s": args.size,
             "elements": ne, "nodes": nn, "init": "LULESH 2.0 (e0=3.948746e7*(s/45)^3)",
             "cycles_per_step": 1, "precision": args.precision,
-            "l2": "no flush: the state (~4.5 GB) is far larger than the 129 MB L2",
+            "l2": "no flush: the state (~5.4 GB) is far larger than the 129 MB L2",
             "parallelism": "replicas" if args.gpus > 1 else "single", "launch": args.launch}
 
 
