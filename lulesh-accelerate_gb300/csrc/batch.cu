@@ -609,7 +609,6 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
         h.courant_key = ~0ULL;
         h.hydro_key = ~0ULL;
         h.elem_begin = (int)eo_i;
-        h.node_begin = (int)no_i;
         iee_h[i] = (int)(eo_i + nei);
         ine_h[i] = (int)(no_i + nni);
         cpos += 8 * nei;

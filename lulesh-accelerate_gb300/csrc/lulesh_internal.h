@@ -44,7 +44,7 @@ struct DevScalars {
     int run_cycles;                      // cycles done by the current lulesh_run
     int run_max;                         // its cap (<= 0: none)
     int geo_valid;                       // Dom::geo holds the current positions' geometry
-    int elem_begin, node_begin;          // first element / node of the instance (batches)
+    int elem_begin;                      // first element of the instance (batches)
     unsigned long long courant_key;      // order-preserving keys of the
     unsigned long long hydro_key;        // constraint minima (see keys below)
 };
