@@ -1,6 +1,6 @@
 // step_fp64.cu -- the plain FP64 Lagrange leapfrog step on sm_103a.
 //
-// One cycle is five launches on one stream:
+// One cycle is six launches on one stream:
 //   k_time_increment   1 thread   TimeIncrement                (LULESH-OMP.cc:557-604)
 //   k_elem_force       1 thr/elem IntegrateStressForElems + CalcHourglassControlForElems
 //                                 + CalcFBHourglassForceForElems, element half
@@ -11,14 +11,17 @@
 //                                 the symmetry-plane conditions, velocity and position
 //                                 (:1613-1683)
 //   k_elem_kinematics  1 thr/elem CalcKinematicsForElems + CalcLagrangeElements +
-//                                 CalcMonotonicQGradientsForElems (:1927-2180)
+//                                 CalcMonotonicQGradientsForElems (:1927-2180); keeps
+//                                 the element geometry (Walsh modes and cross products
+//                                 of the new positions) for the next k_elem_force
 //   k_elem_material    1 thr/elem CalcMonotonicQRegionForElems, the qstop test,
 //                                 ApplyMaterialPropertiesForElems / EvalEOSForElems /
 //                                 CalcEnergyForElems / CalcSoundSpeedForElems,
 //                                 UpdateVolumesForElems and the Courant/hydro
 //                                 constraint minima (:2182-2933)
-//   k_finalize         1 thread   publishes dtcourant/dthydro; in the run loop also
-//                                 decides whether another cycle follows
+//   k_finalize         1 thread   publishes dtcourant/dthydro (k_run_epilogue in the
+//                                 run loop, which also decides whether another cycle
+//                                 follows)
 // No floating-point atomics: node sums run in the reference's fixed corner
 // order and the constraint minima use an order-independent integer min.
 #include "lulesh_internal.h"
