@@ -161,6 +161,33 @@ def test_checkpoint_restart_bitwise(pkg):
     assert got_sc.cycle == want_sc.cycle and got_sc.time == want_sc.time
 
 
+def test_geometry_cache_follows_the_positions(pkg):
+    """The FP64 kinematics kernel keeps each element's geometry for the next
+    force launch; a force launch after positions moved without a kinematics
+    launch in between (LagrangeNodal twice) must form the geometry afresh.
+    A context that reached the same state through an upload (which drops the
+    kept geometry) runs the same phases: both must agree bit for bit, and
+    with the cache used in the first force launch of one of them."""
+    s, k = 8, 30
+    with pkg.Lulesh(s, pkg.INIT_V2) as a:
+        a.run(k)
+        dom = a.download()
+        sc = a.scalars
+        seq = ("time_increment", "lagrange_nodal", "lagrange_nodal", "lagrange_elements",
+               "calc_time_constraints", "time_increment", "lagrange_nodal", "lagrange_elements")
+        for phase in seq:
+            getattr(a, phase)()
+        want = a.download()
+    with pkg.Lulesh(s, pkg.INIT_V2) as b:
+        b.upload(dom)
+        b.scalars = sc
+        for phase in seq:
+            getattr(b, phase)()
+        got = b.download()
+    for x, y in zip(got.arrays(), want.arrays()):
+        assert np.array_equal(x, y)
+
+
 def test_functional_step_matches_reference_api(pkg, orc):
     """lulesh(ctx, domain) -> domain over host arrays (src/LULESH.hs:37-53)."""
     s = 6
