@@ -7,10 +7,12 @@ FP32-level agreement of every phase.
 """
 from __future__ import annotations
 
+import json
+
 import numpy as np
 import pytest
 
-from conftest import find_run, load_phases, rel_err
+from conftest import GOLDEN, find_run, load_phases, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -62,7 +64,10 @@ def test_split_small_ensemble_instances(pkg):
     an FP64 batch: origin energies within the split bar of each other.  An
     approximate FP32 reciprocal root in the characteristic length once moved
     these to 2.2e-6 while the s=30 and s=192 checks stayed green."""
-    sizes, scale = [21, 13, 13, 26, 27, 40], [0.568, 1.704, 1.488, 1.778, 0.514, 1.175]
+    fx = json.loads((GOLDEN / "ensembles.json").read_text())["c4"]
+    pick = [25, 5, 30, 31, 0, 27]          # s = 21, 13, 13, 26, 27, 40
+    sizes = [fx["sizes"][i] for i in pick]
+    scale = [fx["e0_scale"][i] for i in pick]
     e0 = {}
     for name, prec in (("fp64", pkg.FP64), ("split", pkg.SPLIT)):
         with pkg.Batch(sizes, scale, pkg.INIT_V2, prec) as b:
