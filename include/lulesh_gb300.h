@@ -37,7 +37,10 @@ extern "C" {
 #define LULESH_VOLUME_ERROR (-1)   /* LULESH-OMP.cc:82 VolumeError */
 #define LULESH_QSTOP_ERROR  (-2)   /* LULESH-OMP.cc:82 QStopError  */
 #define LULESH_ERR_CUDA     (-3)   /* a CUDA call failed; see lulesh_last_error */
-#define LULESH_ERR_TIMEOUT  (-4)   /* a bounded device wait ran out */
+#define LULESH_ERR_TIMEOUT  (-4)   /* a run stopped short of stoptime: its cycle
+                                      budget ran out, or the time step stopped
+                                      being positive (the reference would loop
+                                      forever); the state stays valid */
 #define LULESH_ERR_ARG      (-5)   /* bad argument */
 
 /* ---- precision of the element kernels -------------------------------- */
@@ -224,8 +227,13 @@ int lulesh_lagrange_leapfrog(lulesh_ctx *ctx);     /* LagrangeLeapFrog   LULESH-
 
 /* The reference's main loop (LULESH-OMP.cc:3179-3188; src/Main.hs:90-108):
  * while (time < stoptime) { TimeIncrement; LagrangeLeapFrog }, at most
- * max_cycles cycles (max_cycles <= 0: no cap).  The loop runs on the device
- * inside one CUDA graph; the host does not wait per cycle. */
+ * max_cycles cycles.  The loop runs on the device inside one CUDA graph; the
+ * host does not wait per cycle.  A device loop always ends: max_cycles <= 0
+ * (or above the budget) means LULESH_RUN_CYCLE_BUDGET cycles, and a run that
+ * stops before stoptime without reaching the caller's own max_cycles -- the
+ * budget ran out, or the time step is no longer positive -- returns
+ * LULESH_ERR_TIMEOUT with the state intact (a further call continues). */
+#define LULESH_RUN_CYCLE_BUDGET (1 << 20)
 int lulesh_run(lulesh_ctx *ctx, int max_cycles, int *cycles_done);
 
 /* Result checks of LULESH-OMP.cc:3197-3223 / src/Main.hs:132-156.  The
@@ -309,15 +317,19 @@ int lulesh_probe_math(double errs[4]);
  * step's time increment; params supplies u_cut and hgcoef.  stream is a
  * cudaStream_t (NULL: the default stream); the call returns after that stream
  * has drained, with LULESH_OK, LULESH_VOLUME_ERROR, or LULESH_ERR_ARG
- * (message on stderr) for a mesh over the limit or an index out of range.
+ * (message on stderr) for a mesh over the limit or malformed tables: an index
+ * out of range, or node-to-corner lists that are not the reference's map
+ * (packed from 0 to 8E, node n's list holding only corners on node n, each
+ * list increasing).  On LULESH_ERR_ARG the state arrays are left unchanged.
  *
  * Its working memory (per-corner forces, node-to-corner slots, the
  * symmetry-plane mask, error words) is one fixed device array compiled into
  * the library: at most 65,536 elements and 131,072 nodes, 14.6 MiB that every
  * GPU on which this call is used keeps until the process exits.  All calls
  * share that array, so calls that overlap on the GPU race; order them on one
- * stream.  The first call on a device looks up the array's address with that
- * device current; make it before any stream capture begins. */
+ * stream.  Every call looks up the array's device address on the calling
+ * thread's current device (a host-side lookup, no allocation); the first call
+ * on a device also loads the library's device code there. */
 int lulesh_lagrange_nodal_noalloc(
     int num_elem, int num_node, double deltatime, const lulesh_params *params,
     const int *nodelist, const int *node_elem_start, const int *node_elem_count,
@@ -348,7 +360,10 @@ const char *lulesh_batch_last_error(const lulesh_batch *b);
 
 /* Run every instance until its time reaches stoptime (the main loop of
  * LULESH-OMP.cc:3179-3188 per instance), at most max_cycles cycles each
- * (<= 0: no cap).  *cycles_done receives the largest per-instance count. */
+ * (<= 0: LULESH_RUN_CYCLE_BUDGET).  *cycles_done receives the largest
+ * per-instance count.  LULESH_ERR_TIMEOUT when an instance without an error
+ * stopped short of stoptime and of the caller's max_cycles (lulesh_run's
+ * rule); an instance's own error is its status in lulesh_batch_instance. */
 int lulesh_batch_run(lulesh_batch *b, int max_cycles, int *cycles_done);
 
 /* Counts; the per-instance state and status (LULESH_OK, LULESH_VOLUME_ERROR

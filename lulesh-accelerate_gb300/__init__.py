@@ -40,6 +40,7 @@ LIB_NAME = "liblulesh_gb300.so"
 
 OK, VOLUME_ERROR, QSTOP_ERROR, ERR_CUDA, ERR_TIMEOUT, ERR_ARG = 0, -1, -2, -3, -4, -5
 FP64, SPLIT = 0, 1
+RUN_CYCLE_BUDGET = 1 << 20   # LULESH_RUN_CYCLE_BUDGET: cycles of a run given no cap
 INIT_V1, INIT_V2 = 1, 2
 
 
@@ -57,6 +58,12 @@ class VolumeError(LuleshError):
 
 class QStopError(LuleshError):
     """Artificial viscosity exceeded qstop (reference exit code -2)."""
+
+
+class RunTimeout(LuleshError):
+    """A run stopped short of stoptime: its cycle budget
+    (``RUN_CYCLE_BUDGET`` when no cap is given) ran out, or the time step
+    stopped being positive.  The state stays valid."""
 
 
 class Parameters(C.Structure):
@@ -202,6 +209,8 @@ def _check(rc: int, handle=None):
         raise VolumeError(rc, msg)
     if rc == QSTOP_ERROR:
         raise QStopError(rc, msg)
+    if rc == ERR_TIMEOUT:
+        raise RunTimeout(rc, msg)
     raise LuleshError(rc, msg)
 
 
@@ -501,6 +510,8 @@ def _check_batch(rc: int, handle=None):
     if rc == OK:
         return
     msg = load_library().lulesh_batch_last_error(handle).decode(errors="replace")
+    if rc == ERR_TIMEOUT:
+        raise RunTimeout(rc, msg)
     raise LuleshError(rc, msg)
 
 

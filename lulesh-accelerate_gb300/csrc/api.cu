@@ -144,6 +144,24 @@ int read_status(lulesh_ctx *ctx)
     return LULESH_OK;
 }
 
+// A run loop that ended with time < stoptime although the caller's own cap
+// was not reached: the cycle budget ran out, or the time step stopped being
+// positive.  Reported, not sticky: the state is valid and a further run
+// continues from it.  Reads the scalars read_status just fetched.
+int short_of_stoptime(lulesh_ctx *ctx, int max_cycles, int done)
+{
+    const DevScalars *h = ctx->h_sc;
+    if (!(h->time < ctx->dom.prm.stoptime)) return LULESH_OK;
+    if (max_cycles > 0 && max_cycles <= kRunCycleLimit && done >= max_cycles) return LULESH_OK;
+    char buf[200];
+    snprintf(buf, sizeof buf, "run stopped at time %.17g < stoptime %.17g after %d cycles: %s", h->time,
+             ctx->dom.prm.stoptime, done,
+             h->deltatime > 0.0 ? "the cycle budget (LULESH_RUN_CYCLE_BUDGET) ran out"
+                                : "the time step is no longer positive");
+    ctx->err = buf;
+    return LULESH_ERR_TIMEOUT;
+}
+
 int check_launch(lulesh_ctx *ctx)
 {
     cudaError_t e = cudaGetLastError();
@@ -800,7 +818,7 @@ int lulesh_run(lulesh_ctx *ctx, int max_cycles, int *cycles_done)
     const int done = ctx->h_sc->run_cycles;
     if (cycles_done) *cycles_done = done;
     ctx->launches += 1 + (long long)done * kernels_per_cycle();
-    return rc;
+    return rc ? rc : short_of_stoptime(ctx, max_cycles, done);
 }
 
 int lulesh_run_profiled(lulesh_ctx *ctx, int max_cycles, int *cycles_done, double *kernel_ms)
@@ -835,7 +853,7 @@ int lulesh_run_profiled(lulesh_ctx *ctx, int max_cycles, int *cycles_done, doubl
     for (auto &e : ev) cudaEventDestroy(e);
     if (!rc) rc = read_status(ctx);
     if (cycles_done) *cycles_done = done;
-    return rc;
+    return rc ? rc : short_of_stoptime(ctx, max_cycles, done);
 }
 
 int lulesh_probe_fp64_peak(double *tflops)

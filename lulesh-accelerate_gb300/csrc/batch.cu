@@ -684,6 +684,17 @@ int lulesh_batch_run(lulesh_batch *b, int max_cycles, int *cycles_done)
     // kernel once per class per cycle
     b->launches += 2 + (long long)most * b->kernels_per_cycle;
     (void)total;
+    // an instance that stopped short of its stop time without an error and
+    // without reaching the caller's cap ran out of cycle budget (or of
+    // positive time step): lulesh_run's LULESH_ERR_TIMEOUT
+    for (int i = 0; i < b->n; ++i) {
+        const DevScalars &h = b->h_sc[i];
+        if (h.err_any || !(h.time < b->dom.prm.stoptime)) continue;
+        if (max_cycles > 0 && max_cycles <= kRunCycleLimit && h.run_cycles >= max_cycles) continue;
+        return bfail(b, LULESH_ERR_TIMEOUT,
+                     "lulesh_batch_run: instance " + std::to_string(i) + " stopped short of stoptime (" +
+                         (h.deltatime > 0.0 ? "cycle budget ran out" : "time step no longer positive") + ")");
+    }
     return LULESH_OK;
 }
 

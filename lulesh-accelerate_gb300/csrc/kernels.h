@@ -39,7 +39,7 @@ void launch_run_prologue(const Dom &d, cudaStream_t st, const int *max_cycles,
 void launch_run_body(const Dom &d, cudaStream_t st, cudaGraphConditionalHandle h, int *active);
 void launch_run_epilogue(const Dom &d, cudaStream_t st, cudaGraphConditionalHandle h, int *active);
 int kernels_per_cycle();
-constexpr int kRunCycleLimit = 1 << 26;
+constexpr int kRunCycleLimit = LULESH_RUN_CYCLE_BUDGET;
 constexpr int kTimedKernels = 6;   // time increment, force, node, kinematics, material, finalize
 void launch_cycle_timed(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTimedKernels + 1]);
 void launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t st);

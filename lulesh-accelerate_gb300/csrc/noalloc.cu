@@ -16,16 +16,19 @@
 //     device memory for the array until the process exits;
 //   - all calls share the one array, so calls that overlap on the GPU (two
 //     streams, or two host threads) race: order them on one stream;
-//   - the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture starts.
+//   - every call looks up the array's device address (cudaGetSymbolAddress,
+//     a host-side lookup that allocates nothing) with the calling thread's
+//     current device, so the address is never stale, whichever context is
+//     current; the first call on a device also loads the library's device
+//     code, and with it the array, onto that device;
+//   - the call reads its status back and waits for its stream before it
+//     returns.
 #include "lulesh_internal.h"
 #include "kernels.h"
 
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 
 namespace lulesh {
 namespace {
@@ -47,9 +50,6 @@ constexpr size_t kScratchBytes = kOffMask + align256(kNoAllocMaxNode);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void *g_scratch_addr[kMaxDevices] = {};
 // Messages go to stderr: this entry point reports through its status code
 // only (it has no context whose lulesh_last_error could carry them).
 int noalloc_fail(int code, const char *msg)
@@ -62,9 +62,19 @@ int noalloc_fail(int code, const char *msg)
 constexpr int kBadInput = 2;
 
 // Per-call preparation, after the scalar block was zeroed: set the time
-// step, check every caller index the step will follow, translate the
-// reference's node-to-corner list (entries 8*elem+corner) into corner-major
-// slots, close the start table and clear the node mask.
+// step, check the caller's mesh tables, translate the reference's
+// node-to-corner list (entries 8*elem+corner) into corner-major slots, close
+// the start table and clear the node mask.
+//
+// The tables must describe the reference's node-to-corner map
+// (AllocateNodeElemIndexes, LULESH-OMP.cc:209-268): every nodelist entry and
+// corner-list entry in range; node n's list is corner_list[start[n] ..
+// start[n] + count[n]), the lists packed back to back from 0 to 8E; every
+// entry of node n's list a corner whose nodelist entry is n; and each list
+// strictly increasing, as the reference builds it.  Together these make the
+// lists a permutation of the 8E corners, so the gather sums every corner
+// force exactly once.  A table that breaks any of them marks kBadInput and
+// the step kernels then read nothing through it.
 __global__ void k_noalloc_prepare(DevScalars *sc, double deltatime, const int *nodelist,
                                   const int *corner_list_ref, int *slots, const int *start_ref,
                                   const int *count_ref, int *start, unsigned char *mask, int ne, int nn)
@@ -75,7 +85,7 @@ __global__ void k_noalloc_prepare(DevScalars *sc, double deltatime, const int *n
         sc->deltatime = deltatime;
         const long end = (long)start_ref[nn - 1] + count_ref[nn - 1];
         start[nn] = (int)end;
-        if (end != nc) sc->err_any = kBadInput;
+        if (end != nc || start_ref[0] != 0) sc->err_any = kBadInput;
     }
     if (i < nc) {
         const int k = corner_list_ref[i];
@@ -89,7 +99,15 @@ __global__ void k_noalloc_prepare(DevScalars *sc, double deltatime, const int *n
     }
     if (i < nn) {
         const int st = start_ref[i], cnt = count_ref[i];
-        if (st < 0 || cnt < 0 || (long)st + cnt > nc) sc->err_any = kBadInput;
+        bool bad = st < 0 || cnt < 0 || (long)st + cnt > nc;
+        if (!bad && i + 1 < nn) bad = (long)st + cnt != (long)start_ref[i + 1];
+        // the node's own list: in range, its corners on this node, increasing
+        for (int j = 0, prev = -1; !bad && j < cnt; ++j) {
+            const int k = corner_list_ref[st + j];
+            bad = k <= prev || k >= nc || nodelist[k] != (int)i;
+            prev = k;
+        }
+        if (bad) sc->err_any = kBadInput;
         start[i] = st;
         mask[i] = 0;
     }
@@ -146,23 +164,13 @@ extern "C" int lulesh_lagrange_nodal_noalloc(
         return noalloc_fail(LULESH_ERR_ARG, "missing array");
     const bool keep = fx && fy && fz;
 
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    // the array's device address on the current device and context (its
+    // host-side name is only a stand-in); looked up on every call, so a
+    // reset device or another context never leaves a stale address behind
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess) return noalloc_fail(LULESH_ERR_CUDA, cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(LULESH_ERR_ARG, "device ordinal out of range");
-    unsigned char *base = nullptr;
-    {
-        // once per device, with that device current: the array's device
-        // address (its host-side name is only a stand-in)
-        std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_addr[dev]) {
-            void *ptr = nullptr;
-            e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-            if (e != cudaSuccess) return noalloc_fail(LULESH_ERR_CUDA, cudaGetErrorString(e));
-            g_scratch_addr[dev] = ptr;
-        }
-        base = static_cast<unsigned char *>(g_scratch_addr[dev]);
-    }
+    unsigned char *base = static_cast<unsigned char *>(ptr);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const size_t ne = (size_t)num_elem;
 
@@ -214,7 +222,9 @@ extern "C" int lulesh_lagrange_nodal_noalloc(
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return noalloc_fail(LULESH_ERR_CUDA, cudaGetErrorString(e));
     if (h.err_any == kBadInput)
-        return noalloc_fail(LULESH_ERR_ARG, "a node, corner or start index is out of range");
+        return noalloc_fail(LULESH_ERR_ARG,
+                            "malformed mesh tables (an index out of range, or node-to-corner lists "
+                            "that are not the reference's packed, increasing map)");
     if (h.err[ERR_K1_DETERM] || h.err[ERR_K1_VOLUME]) return LULESH_VOLUME_ERROR;
     return LULESH_OK;
 }

@@ -16,10 +16,15 @@
  *   - an unstructured mesh read from a .lmesh file (-u FILE), set up as the
  *     reference's unstructured reader does
  *     (reference/CUDA/lulesh-kepler-singlegpu/lulesh.cu:733-923, restated);
- *   - a cycle cap, full-precision JSON output and binary state dumps.
+ *   - an energy factor (--efactor F) that multiplies the LULESH 2.0 initial
+ *     energy before dt0 is formed from it, as the seeded ensembles draw it;
+ *   - a cycle cap, full-precision JSON output and binary state dumps;
+ *   - the whole-problem results of the final state (total energy, largest
+ *     nodal speed, viscosity-weighted shock radius; the definitions of the
+ *     package's sedov_metrics), so long runs need no state dump.
  *
- * Usage: lulesh_ref S [--init v1|v2] [--cycles N] [--warmup W] [--dump FILE]
- *                     [--phase-dump FILE CYCLE]
+ * Usage: lulesh_ref S [--init v1|v2] [--efactor F] [--cycles N] [--warmup W]
+ *                     [--dump FILE] [--phase-dump FILE CYCLE]
  *        lulesh_ref -u FILE.lmesh [--cycles N] [--warmup W] [--dump FILE]
  *                     [--phase-dump FILE CYCLE]
  * (--warmup W: the first W cycles run before the timer starts; they count
@@ -82,7 +87,7 @@ void dump(FILE *f, int stage)
 }
 
 /* Mesh and state set-up: the reference main() :2960-3171 restated. */
-void setup(Index_t edgeElems, bool v2)
+void setup(Index_t edgeElems, bool v2, Real_t efactor)
 {
     const Index_t edgeNodes = edgeElems + 1;
     domain.sizeX() = edgeElems;
@@ -173,7 +178,7 @@ void setup(Index_t edgeElems, bool v2)
     if (v2) {
         const Real_t ebase = Real_t(3.948746e+7);
         const Real_t scale = Real_t(edgeElems) / Real_t(45.0);
-        const Real_t einit = ebase * scale * scale * scale;
+        const Real_t einit = ebase * scale * scale * scale * efactor;
         domain.e(0) = einit;
         domain.deltatime() = (Real_t(.5) * cbrt(domain.volo(0))) / sqrt(Real_t(2.0) * einit);
     } else {
@@ -373,6 +378,38 @@ Index_t setup_unstructured(const char *path)
     return origin;
 }
 
+/* Whole-problem results of the current state: internal plus kinetic energy
+ * sum(e m_elem) + sum(m_node |v|^2)/2, the largest nodal speed, and the
+ * mean radius of the element centroids weighted by q m_elem (q is non-zero
+ * only in the compression zone, so the mean follows the shock front). */
+struct Metrics { double total_energy, max_velocity, shock_radius; };
+
+Metrics metrics()
+{
+    double eint = 0.0, ekin = 0.0, vmax2 = 0.0, wr = 0.0, w = 0.0;
+    for (Index_t n = 0; n < domain.numNode(); ++n) {
+        const double v2 = double(domain.xd(n)) * domain.xd(n) + double(domain.yd(n)) * domain.yd(n) +
+                          double(domain.zd(n)) * domain.zd(n);
+        ekin += 0.5 * domain.nodalMass(n) * v2;
+        if (v2 > vmax2) vmax2 = v2;
+    }
+    for (Index_t k = 0; k < domain.numElem(); ++k) {
+        eint += double(domain.e(k)) * domain.elemMass(k);
+        const Index_t *l = domain.nodelist(k);
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        for (int c = 0; c < 8; ++c) { cx += domain.x(l[c]); cy += domain.y(l[c]); cz += domain.z(l[c]); }
+        cx /= 8.0; cy /= 8.0; cz /= 8.0;
+        const double qm = double(domain.q(k)) * domain.elemMass(k);
+        wr += sqrt(cx * cx + cy * cy + cz * cz) * qm;
+        w += qm;
+    }
+    Metrics m;
+    m.total_energy = eint + ekin;
+    m.max_velocity = sqrt(vmax2);
+    m.shock_radius = w > 0.0 ? wr / w : 0.0;
+    return m;
+}
+
 }  // namespace
 
 int main(int argc, char *argv[])
@@ -387,10 +424,12 @@ int main(int argc, char *argv[])
     const int s = unstructured ? 0 : atoi(argv[1]);
     bool v2 = true;
     int max_cycles = 0, phase_cycle = -1, warmup = 0;
+    Real_t efactor = Real_t(1.0);
     const char *dump_path = NULL, *phase_path = NULL;
     for (int i = unstructured ? 3 : 2; i < argc; ++i) {
         if (!strcmp(argv[i], "--init") && i + 1 < argc) v2 = strcmp(argv[++i], "v1") != 0;
         else if (!strcmp(argv[i], "--cycles") && i + 1 < argc) max_cycles = atoi(argv[++i]);
+        else if (!strcmp(argv[i], "--efactor") && i + 1 < argc) efactor = Real_t(strtod(argv[++i], NULL));
         else if (!strcmp(argv[i], "--warmup") && i + 1 < argc) warmup = atoi(argv[++i]);
         else if (!strcmp(argv[i], "--dump") && i + 1 < argc) dump_path = argv[++i];
         else if (!strcmp(argv[i], "--phase-dump") && i + 2 < argc) {
@@ -406,8 +445,8 @@ int main(int argc, char *argv[])
         origin = setup_unstructured(argv[2]);
         v2 = false;
     } else {
-        if (s < 1) return 2;
-        setup(s, v2);
+        if (s < 1 || !(efactor > Real_t(0.))) return 2;
+        setup(s, v2, efactor);
     }
 
     FILE *pf = phase_path ? fopen(phase_path, "wb") : NULL;
@@ -446,6 +485,7 @@ int main(int argc, char *argv[])
             const Real_t r = a / domain.e(k * s + j);
             if (MaxRelDiff < r) MaxRelDiff = r;
         }
+    const Metrics mt = metrics();
     if (dump_path) {
         FILE *f = fopen(dump_path, "wb");
         if (f) { dump(f, 9); fclose(f); }
@@ -455,10 +495,12 @@ int main(int argc, char *argv[])
     printf("{\"s\": %d, \"init\": \"%s\", \"origin_elem\": %d, \"num_elem\": %d, \"cycles\": %d, \"origin_energy\": %.17e, "
            "\"time\": %.17e, \"deltatime\": %.17e, \"dtcourant\": %.17e, \"dthydro\": %.17e, "
            "\"max_abs_diff\": %.17e, \"total_abs_diff\": %.17e, \"max_rel_diff\": %.17e, "
+           "\"total_energy\": %.17e, \"max_velocity\": %.17e, \"shock_radius\": %.17e, "
            "\"elapsed_s\": %.6f, \"timed_cycles\": %d, \"threads\": %d, \"mzone_cycles_per_s\": %.6f}\n",
            s, v2 ? "v2" : "v1", int(origin), int(domain.numElem()), domain.cycle(), double(domain.e(origin)), double(domain.time()),
            double(domain.deltatime()), double(domain.dtcourant()), double(domain.dthydro()),
-           double(MaxAbsDiff), double(TotalAbsDiff), double(MaxRelDiff), elapsed, timed,
+           double(MaxAbsDiff), double(TotalAbsDiff), double(MaxRelDiff),
+           mt.total_energy, mt.max_velocity, mt.shock_radius, elapsed, timed,
            omp_get_max_threads(), elapsed > 0 ? zc / elapsed * 1e-6 : 0.0);
     return 0;
 }

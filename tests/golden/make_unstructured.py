@@ -20,12 +20,16 @@ This script
   ``phases_sedov15oct_c80.npz``.
 
 Needs the reference tree and its build (``make -C oracle``).
-Usage: ``python tests/golden/make_unstructured.py``.
+Usage: ``python tests/golden/make_unstructured.py [REFERENCE_ROOT]``; the
+reference tree's root comes from the argument, else from the environment
+variable ``REF_ROOT`` (the name ``oracle/Makefile`` uses), else
+``/root/reference``.
 """
 from __future__ import annotations
 
 import gzip
 import json
+import os
 import sys
 import tempfile
 from pathlib import Path
@@ -37,7 +41,8 @@ sys.path.insert(0, str(ROOT / "oracle"))
 import oracle  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
-KEPLER = Path("/root/reference/reference/CUDA/lulesh-kepler-singlegpu")
+REF_ROOT = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REF_ROOT", "/root/reference"))
+KEPLER = REF_ROOT / "reference" / "CUDA" / "lulesh-kepler-singlegpu"
 MESHES = ("sedov15oct", "sedov21oct")
 PHASE_MESH, PHASE_CYCLE = "sedov15oct", 80
 SAMPLE_STRIDE = 97

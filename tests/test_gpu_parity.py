@@ -224,6 +224,31 @@ def test_qstop_error(pkg):
             g.run(20)
 
 
+def test_run_short_of_stoptime_is_reported(pkg):
+    """A time step that is no longer positive would keep the reference's main
+    loop (LULESH-OMP.cc:3179-3188) spinning forever; the device loop stops at
+    once and the run reports LULESH_ERR_TIMEOUT, through the run graph and the
+    kernel-by-kernel loop, with the state left as it was.  A caller's own cap
+    is not an error."""
+    with pkg.Lulesh(5, pkg.INIT_V2) as g:
+        assert g.run(3) == 3
+        sc = g.scalars
+        x0 = g.get_field("x")
+        sc.deltatime = 0.0
+        g.scalars = sc
+        with pytest.raises(pkg.RunTimeout):
+            g.run()
+        with pytest.raises(pkg.RunTimeout):
+            g.run(5)
+        with pytest.raises(pkg.RunTimeout):
+            g.run_profiled()
+        assert g.scalars.cycle == 3
+        np.testing.assert_array_equal(g.get_field("x"), x0)
+    with pkg.Lulesh(5, pkg.INIT_V2) as g:
+        assert g.run(7) == 7
+        assert g.run_profiled(2)[0] == 2
+
+
 def test_large_mesh_matches_oracle(pkg, orc):
     """s=192 (the headline mesh): three full cycles against the oracle."""
     s, n = 192, 3

@@ -95,6 +95,100 @@ def test_noalloc_nodal_matches_context_path(pkg):
             g.calc_time_constraints()
 
 
+def _bind(pkg):
+    fn = pkg.load_library().lulesh_lagrange_nodal_noalloc
+    fn.restype = C.c_int
+    fn.argtypes = ([C.c_int, C.c_int, C.c_double, C.POINTER(pkg.Parameters)] + [C.c_void_p] * 7 +
+                   [C.c_int] + [C.c_void_p] * 16 + [C.c_void_p])
+    return fn
+
+
+def _call_fresh(pkg, s, edit=None):
+    """One call on the initial s^3 Sedov state after ``edit(arrays)`` changed
+    the host arrays; returns the status and the state before/after."""
+    torch = pytest.importorskip("torch")
+    fn = _bind(pkg)
+    dev = torch.device("cuda", 0)
+    mesh = pkg.mesh_build(s, pkg.INIT_V2)
+    ne, nn = pkg.mesh_sizes(s)
+    sx, sy, sz = _symm_sets(s)
+    host = {k: np.array(mesh[k], dtype=np.int32) for k in
+            ("nodelist", "node_elem_start", "node_elem_count", "node_elem_corner_list")}
+    host.update({k: np.array(mesh[k], dtype=np.float64) for k in ("volo", "elem_mass", "nodal_mass")})
+    host.update({"sx": sx, "sy": sy, "sz": sz})
+    host.update({k: np.array(mesh[k], dtype=np.float64) for k in ("x", "y", "z")})
+    host.update({k: np.zeros(nn) for k in ("xd", "yd", "zd")})
+    host.update({"p": np.zeros(ne), "q": np.zeros(ne), "v": np.ones(ne), "ss": np.zeros(ne)})
+    host["xd"][nn - 1] = 1.0   # some motion, so that an unchanged state says something
+    if edit is not None:
+        edit(host)
+    dv = {k: torch.as_tensor(np.ascontiguousarray(a)).to(dev) for k, a in host.items()}
+    f = [torch.zeros(nn, dtype=torch.float64, device=dev) for _ in range(3)]
+    params = pkg.default_parameters()
+    ptr = {k: t.data_ptr() for k, t in dv.items()}
+    rc = fn(ne, nn, 1e-7, C.byref(params), ptr["nodelist"], ptr["node_elem_start"],
+            ptr["node_elem_count"], ptr["node_elem_corner_list"], ptr["sx"], ptr["sy"], ptr["sz"],
+            len(sx), ptr["volo"], ptr["elem_mass"], ptr["nodal_mass"], ptr["p"], ptr["q"], ptr["v"],
+            ptr["ss"], ptr["x"], ptr["y"], ptr["z"], ptr["xd"], ptr["yd"], ptr["zd"],
+            f[0].data_ptr(), f[1].data_ptr(), f[2].data_ptr(), None)
+    torch.cuda.synchronize(dev)
+    after = {k: dv[k].cpu().numpy() for k in ("x", "y", "z", "xd", "yd", "zd")}
+    return rc, host, after
+
+
+def test_noalloc_good_tables_step(pkg):
+    rc, before, after = _call_fresh(pkg, 3)
+    assert rc == pkg.OK
+    # the moving node moved
+    assert after["x"][-1] != before["x"][-1]
+
+
+@pytest.mark.parametrize("case", ["corner_out_of_range", "start_count_gap", "corner_of_other_node",
+                                  "corner_repeated", "nodelist_out_of_range"])
+def test_noalloc_rejects_malformed_tables(pkg, case):
+    """Tables that are in bounds but do not describe the reference's
+    node-to-corner map are refused before any step kernel reads through them:
+    the call returns LULESH_ERR_ARG and leaves the state as it was."""
+    s = 3
+    ne = s ** 3
+
+    def edit(h):
+        cl, st, cnt = h["node_elem_corner_list"], h["node_elem_start"], h["node_elem_count"]
+        if case == "corner_out_of_range":
+            cl[5] = 8 * ne
+        elif case == "start_count_gap":
+            # node 1's list starts one slot late: the lists no longer pack
+            st[1] += 1
+            cnt[1] -= 1
+        elif case == "corner_of_other_node":
+            # node 0's single corner swapped for one of node 1's
+            cl[st[0]], cl[st[1]] = cl[st[1]], cl[st[0]]
+        elif case == "corner_repeated":
+            # a corner listed twice by its node, another of its corners dropped
+            n = int(np.argmax(cnt))
+            cl[st[n] + 1] = cl[st[n]]
+        elif case == "nodelist_out_of_range":
+            h["nodelist"][7] = -1
+
+    rc, before, after = _call_fresh(pkg, s, edit)
+    assert rc == pkg.ERR_ARG, rc
+    for k in after:
+        np.testing.assert_array_equal(after[k], before[k], err_msg=k)
+
+
+def test_noalloc_volume_error(pkg):
+    """A relative volume of 0 is the reference's VolumeError
+    (CalcHourglassControlForElems, LULESH-OMP.cc:1541-1543); the nodes do not
+    move."""
+    def edit(h):
+        h["v"][4] = 0.0
+
+    rc, before, after = _call_fresh(pkg, 3, edit)
+    assert rc == pkg.VOLUME_ERROR, rc
+    for k in after:
+        np.testing.assert_array_equal(after[k], before[k], err_msg=k)
+
+
 def test_noalloc_rejects_oversized_mesh(pkg):
     torch = pytest.importorskip("torch")
     lib = pkg.load_library()
