@@ -51,9 +51,36 @@ UNIT = "Mzone-cycles/s"
 KERNELS = ("time_increment", "elem_force", "node_update", "elem_kinematics", "elem_material", "finalize")
 
 
+# The step's compulsory DRAM traffic in its three-kernel form (8-byte doubles,
+# 4-byte indices and floats, every array touched once):
+#   K1 element forces: x..zd gathered (48/node), nodelist (32/elem),
+#      p q v volo ss elemMass (48/elem) in; 24 corner forces out (192/elem,
+#      96 in FP32)
+#   K2 node update: start+count (8/node), corner list (32/elem), the corner
+#      forces (192/elem, 96 in FP32), nodalMass (8/node), x..zd read and
+#      written (96/node)
+#   K3 element update: nodelist (32/elem), x..zd gathered (48/node), v volo
+#      elemMass e p q (48/elem) in; e p q v ss (40/elem) out
+# FP64: 616 E + 208 N bytes per cycle (827.3 per zone-cycle at s=192); split
+# precision with FP32 corner forces: 424 E + 208 N (635.3).
+SECTION8_KERNELS = {"elem_force": "K1", "node_update": "K2", "elem_kinematics": "K3", "elem_material": "K3"}
+
+
+def step_bytes(ne: int, nn: int, precision: str = "fp64") -> dict:
+    """Algorithmic bytes per cycle of K1, K2 and K3 (the step's compulsory
+    traffic, independent of how this library splits and caches it)."""
+    corner = 192 if precision == "fp64" else 96
+    return {"K1": 48 * nn + (32 + 48 + corner) * ne,
+            "K2": (8 + 8 + 96) * nn + (32 + corner) * ne,
+            "K3": 48 * nn + (32 + 48 + 40) * ne}
+
+
 def algorithmic_bytes(ne: int, nn: int, precision: str = "fp64") -> dict:
-    """Compulsory DRAM bytes per launch of each kernel (8-byte doubles,
-    4-byte floats and indices, every array touched once)."""
+    """Compulsory DRAM bytes per launch of each of this library's kernels
+    (8-byte doubles, 4-byte floats and indices, every array touched once),
+    including what its own design adds to the step's traffic: the geometry
+    cache, reciprocal masses and volumes, the Q gradients handed from the
+    kinematics to the material kernel."""
     if precision == "split":
         return {
             "time_increment": 0,
@@ -200,13 +227,59 @@ def regions_leg(pkg, args, timed, plain_value) -> dict:
             "vs_plain_fp64": value / plain_value, "gpu_launches": launches}
 
 
-def batch_legs(pkg, torch, args, barrier, max_over_ranks) -> dict:
+def load_reference_runs() -> dict:
+    """The unmodified reference's answers for the full-length runs and the
+    seeded ensembles (tests/golden/reference_runs.json, made by
+    tests/golden/make_reference_runs.py)."""
+    p = ROOT / "tests" / "golden" / "reference_runs.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def accuracy_vs_reference(pkg, precision, mesh, ref: dict) -> dict:
+    """The s=192 problem run from its initial state for the reference's own
+    cycle count (500): relative errors of the four whole-problem results and
+    of the time against the unmodified reference's run of the same cycles."""
+    with pkg.Lulesh(ref["s"], pkg.INIT_V2, precision) as g:
+        n = g.run(ref["cycles"])
+        got = pkg.sedov_metrics(g, mesh)
+        sc = g.scalars
+        sym = g.symmetry()
+    want = {k: ref[k] for k in ("origin_energy", "total_energy", "max_velocity", "shock_radius")}
+    errs = pkg.relative_errors(got, want)
+    errs["time"] = abs(sc.time - ref["time"]) / ref["time"]
+    return {"cycles": n, "cycles_equal": n == ref["cycles"] and sc.cycle == ref["cycles"], "errors": errs,
+            "plane0_max_rel_diff": sym[2], "reference_plane0_max_rel_diff": ref["max_rel_diff"],
+            "reference": "tests/golden/reference_runs.json s192_c500 (LULESH-OMP.cc, 500 cycles)"}
+
+
+SIZE_BANDS = ((1, 24), (25, 40), (41, 56), (57, 64), (65, 1 << 30))
+
+
+def spread_order(n: int) -> list[int]:
+    """0..n-1 visited middle first, then quarters, eighths, ...: a sample that
+    stops early still spans the range."""
+    order, seen, k = [], set(), 1
+    while len(order) < n:
+        for j in range(k):
+            i = min(n - 1, int((2 * j + 1) * n / (2 * k)))
+            if i not in seen:
+                seen.add(i)
+                order.append(i)
+        k *= 2
+    return order
+
+
+def batch_legs(pkg, torch, args, barrier, max_over_ranks, ref_runs: dict) -> dict:
     """Configs 3 and 4: seeded ensembles run to t = 1e-2 in one captured graph
     (c3: 64 instances, plain FP64; c4: 528 instances, split precision),
-    against the same instances run one at a time on the plain FP64 path
-    (a time-bounded sample of them, since the rate is what is compared)."""
-    import numpy as np
+    against the same instances run one at a time on the plain FP64 path, and
+    every instance's result against the reference's own run of it.
 
+    The one-at-a-time rate is sampled per size band (SIZE_BANDS), at least
+    one instance each, spread over the band's sizes, and the bands are
+    weighted by their share of the ensemble's zone-cycles: the time the
+    instances would take one after another is sum(band zone-cycles / band
+    rate)."""
     fx = json.loads((ROOT / "tests" / "golden" / "ensembles.json").read_text())
     cache = ROOT / "lulesh-accelerate_gb300" / "_build" / "batch_tuning.json"
     cache.parent.mkdir(exist_ok=True)
@@ -235,11 +308,8 @@ def batch_legs(pkg, torch, args, barrier, max_over_ranks) -> dict:
         tuning = b.tuning()
         b.close()
 
-        # one at a time on the plain FP64 path: instances in order until the
-        # sample has run for --solo-seconds
-        solo_zc = solo_ms = 0.0
-        solo_n = 0
-        for i in range(len(sizes)):
+        # one at a time on the plain FP64 path, sampled per size band
+        def solo(i):
             g = pkg.Lulesh(int(sizes[i]), pkg.INIT_V2, pkg.FP64)
             e = np.zeros(int(sizes[i]) ** 3)
             e[0] = init[i][1]
@@ -253,35 +323,53 @@ def batch_legs(pkg, torch, args, barrier, max_over_ranks) -> dict:
             n = g.run()
             a1.record(gst)
             torch.cuda.synchronize()
-            solo_ms += a0.elapsed_time(a1)
-            solo_zc += float(sizes[i]) ** 3 * n
-            solo_n += 1
             g.close()
-            if solo_ms > 1e3 * args.solo_seconds:
-                break
-        solo_rate = solo_zc / (solo_ms * 1e-3) * 1e-6
+            return float(sizes[i]) ** 3 * n, a0.elapsed_time(a1)
+
+        bands = []
+        banded = [((lo, hi), sorted((i for i, x in enumerate(sizes) if lo <= x <= hi), key=lambda i: (sizes[i], i)))
+                  for lo, hi in SIZE_BANDS]
+        banded = [(bd, m) for bd, m in banded if m]
+        budget_ms = 1e3 * args.solo_seconds / len(banded)
+        est_ms = 0.0
+        for (lo, hi), m in banded:
+            band_zc = sum(float(sizes[i]) ** 3 * final[i][0].cycle for i in m)
+            s_zc = s_ms = 0.0
+            picked = []
+            for j in spread_order(len(m)):
+                z, t = solo(m[j])
+                s_zc, s_ms = s_zc + z, s_ms + t
+                picked.append(int(sizes[m[j]]))
+                if s_ms > budget_ms:
+                    break
+            rate = s_zc / (s_ms * 1e-3) * 1e-6
+            est_ms += band_zc / (rate * 1e6) * 1e3
+            bands.append({"sizes": [lo, min(hi, max(sizes))], "instances": len(m), "sampled_sizes": picked,
+                          "zone_cycle_share": band_zc / zc, "value": rate})
+        solo_rate = zc / (est_ms * 1e-3) * 1e-6
         value = zc / (ms * 1e-3) * 1e-6
         leg = {"instances": len(sizes), "precision": prec_name, "elements": int(sum(int(x) ** 3 for x in sizes)),
                "seed": fx[name]["seed"], "cycles_max": most, "zone_cycles": zc, "ms": ms,
                "value": value, "unit": UNIT, "instances_per_s": len(sizes) / (ms * 1e-3),
-               "one_at_a_time_fp64": {"value": solo_rate, "unit": UNIT, "instances_sampled": solo_n,
-                                      "ms": solo_ms},
+               "one_at_a_time_fp64": {"value": solo_rate, "unit": UNIT, "bands": bands,
+                                      "weighting": "each size band's sampled rate weighted by the band's share "
+                                                   "of the ensemble's zone-cycles"},
                "speedup_vs_one_at_a_time_fp64": value / solo_rate, "gpu_launches": launches,
                "autotuned": tuning}
 
-        if prec_name == "split":
-            # per-instance origin-energy error against FP64: one s=96
-            # instance and the first 32 smaller ones, run as an FP64 batch
-            idx = [i for i, x in enumerate(sizes) if x <= 48][:32] + [i for i, x in enumerate(sizes) if x > 48][:1]
-            with pkg.Batch([sizes[i] for i in idx], [scale[i] for i in idx], pkg.INIT_V2, pkg.FP64) as r:
-                r.autotune(str(cache))
-                r.run()
-                errs = []
-                for j, i in enumerate(idx):
-                    rsc, re0, _ = r.instance(j)
-                    errs.append(abs(final[i][1] - re0) / abs(re0))
-            leg["origin_energy_error_vs_fp64"] = {"max": max(errs), "median": float(np.median(errs)),
-                                                   "instances_compared": len(idx)}
+        # every instance the reference ran, against its own answer
+        refs = ref_runs.get(name, [])
+        if refs:
+            errs, cyc_diff = [], []
+            for r in refs:
+                i = r["index"]
+                errs.append(abs(final[i][1] - r["origin_energy"]) / abs(r["origin_energy"]))
+                cyc_diff.append(final[i][0].cycle - r["cycles"])
+            leg["origin_energy_error_vs_reference"] = {
+                "max": max(errs), "median": float(np.median(errs)), "instances_compared": len(refs),
+                "instances_with_other_cycle_count": int(sum(1 for d in cyc_diff if d)),
+                "largest_cycle_difference": int(max(abs(d) for d in cyc_diff)),
+                "reference": f"tests/golden/reference_runs.json {name} (LULESH-OMP.cc per instance)"}
         out[name] = leg
     return out
 
@@ -326,9 +414,9 @@ def run_reference(args, world, rank):
     ne, nn = args.size ** 3, (args.size + 1) ** 3
     threads = os.cpu_count() or 1
     n = max(1, min(args.steps, args.cpu_cycles))
-    cb = cpu_run(args.size, min(args.warmup, 2), n, threads)
+    cb = cpu_run(args.size, args.warmup, n, threads)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": cb["cycles"], "warmup": min(args.warmup, 2),
+            "steps": cb["cycles"], "warmup": args.warmup,
             "ms_per_step": 1e3 * cb["elapsed_s"] / max(cb["cycles"], 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_for(args, ne, nn),
@@ -347,6 +435,10 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
     ap.add_argument("--profile-cycles", type=int, default=20)
     ap.add_argument("--e2e-cycles", type=int, default=0, help="0: same as --steps")
+    ap.add_argument("--copy-cycles", type=int, default=20,
+                    help="cycles of the e2e variant that copies the whole Domain every cycle")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the 500-cycle runs compared with the reference's own")
     ap.add_argument("--cpu-cycles", type=int, default=40,
                     help="cycles of the CPU baseline sample (about 10 s of the 16-core host at s=192)")
     ap.add_argument("--no-cpu", action="store_true")
@@ -412,13 +504,18 @@ def main():
 
     def kernel_table(ctx, precision):
         """Per-kernel device time from a kernel-by-kernel pass, the roofline
-        of the dominant kernel, and the algorithmic bytes per zone-cycle."""
+        of the dominant kernel against the step's algorithmic bytes (K1, K2,
+        K3), and the bytes per zone-cycle."""
         pc, kms = ctx.run_profiled(args.profile_cycles)
         per_launch = {k: v / max(pc, 1) for k, v in kms.items()}
         abytes = algorithmic_bytes(ne, nn, precision)
+        sbytes = step_bytes(ne, nn, precision)
         peaks = measured_peaks()
         top = max(("elem_force", "node_update", "elem_kinematics", "elem_material"), key=lambda k: per_launch[k])
-        achieved = abytes[top] / (per_launch[top] * 1e-3) * 1e-9
+        part = SECTION8_KERNELS[top]
+        part_ms = sum(per_launch[k] for k, v in SECTION8_KERNELS.items() if v == part)
+        achieved = sbytes[part] / (part_ms * 1e-3) * 1e-9
+        design_achieved = abytes[top] / (per_launch[top] * 1e-3) * 1e-9
         traffic = None
         fp64 = None
         tf = ROOT / "profiles" / "traffic.json"
@@ -439,15 +536,24 @@ def main():
                             "issue_frac": inst_rate / slot_rate,
                             "peak_source": "measured FP64 FMA probe (lulesh_probe_fp64_peak)",
                             "flops_source": "per-unit FP64 work from the ncu capture in profiles/traffic.json"}
-        roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+        roof = {"bound": "hbm", "kernel": top, "step_kernel": part, "achieved": achieved, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                 "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
-                "algorithmic_bytes_per_launch": abytes[top], "fp64_issue": fp64}
+                "algorithmic_bytes_per_launch": sbytes[part],
+                "algorithmic_bytes_source": f"the step's {part} traffic (48/node gathered, 4-byte indices, "
+                                            "8-byte doubles; FP32 corner forces in split precision)",
+                "design_bytes_per_launch": abytes[top], "design_achieved": design_achieved,
+                "design_frac": design_achieved / peaks["hbm_gbs"], "fp64_issue": fp64}
         total = sum(per_launch.values())
         table = {k: {"ms": per_launch[k], "share": per_launch[k] / total,
-                     "gbs": abytes[k] / (per_launch[k] * 1e-3) * 1e-9 if per_launch[k] > 0 else 0.0}
+                     "design_gbs": abytes[k] / (per_launch[k] * 1e-3) * 1e-9 if per_launch[k] > 0 else 0.0}
                  for k in KERNELS}
-        return roof, table, sum(abytes.values()) / ne
+        cycle = {"bytes_per_zone_cycle": sum(sbytes.values()) / ne,
+                 "design_bytes_per_zone_cycle": sum(abytes.values()) / ne,
+                 "design_added_bytes_per_zone_cycle": (sum(abytes.values()) - sum(sbytes.values())) / ne}
+        if precision == "fp64":
+            cycle["geometry_cache_bytes_per_zone_cycle"] = 2 * 39 * 8
+        return roof, table, cycle
 
     mesh = pkg.mesh_build(args.size, pkg.INIT_V2)
     fp64_peak = pkg.probe_fp64_peak()
@@ -456,10 +562,13 @@ def main():
     clocks = ClockSampler(local)
     ms, launches = timed(g, args.steps, clocks)       # already the slowest rank's time
     value = world * ne * args.steps / (ms * 1e-3) * 1e-6
-    ref_metrics = pkg.sedov_metrics(g, mesh)          # state after W + K cycles
     roofline, kernels, cycle_bytes = kernel_table(g, args.precision)
 
     # ---- end to end through the C ABI with host buffers -------------------
+    # (a) resident state, as a host that keeps its Domain on the device: the
+    #     state goes up once before the first cycle and comes back once after
+    #     the last; every cycle is two ABI calls, each returning its status
+    #     (a 40-byte scalar read)
     e2e_cycles = args.e2e_cycles or args.steps
     pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
     host = pkg.Domain.empty(ne, nn, pinned=pin)
@@ -476,12 +585,41 @@ def main():
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e_value = world * ne * e2e_cycles / e2e_s * 1e-6
+    # (b) the whole Domain across the FFI every cycle, as the functional step
+    #     lulesh(domain) -> domain' of the Haskell host: upload, two calls,
+    #     download, per cycle
+    copy_cycles = max(1, min(args.copy_cycles, e2e_cycles))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(copy_cycles):
+        g.upload(host)
+        g.time_increment()
+        g.lagrange_leapfrog()
+        g.download(host)
+    barrier()
+    copy_s = max_over_ranks(time.perf_counter() - t0)
     e2e = {"value": e2e_value, "unit": UNIT, "cycles": e2e_cycles,
            "h2d_bytes_per_step": state_bytes / e2e_cycles,
            "d2h_bytes_per_step": (state_bytes + 2 * scalar_bytes * e2e_cycles) / e2e_cycles,
-           "timer": "host wall clock around upload + per-cycle ABI calls + download"}
+           "copies": "resident state: the Domain is uploaded once before the first cycle and downloaded once "
+                     "after the last (bytes per step are those two copies spread over the cycles); every cycle "
+                     "is a lulesh_time_increment + lulesh_lagrange_leapfrog call pair, each reading back its status",
+           "timer": "host wall clock around upload + per-cycle ABI calls + download",
+           "state_copied_every_cycle": {
+               "value": world * ne * copy_cycles / copy_s * 1e-6, "unit": UNIT, "cycles": copy_cycles,
+               "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes + 2 * scalar_bytes,
+               "copies": "the whole Domain uploaded from pinned memory and downloaded every cycle"}}
     del host
     g.close()
+
+    # ---- results at cycle 500 against the reference's own 500-cycle run ----
+    ref_runs = load_reference_runs()
+    accuracy = {}
+    if args.size == 192 and "s192_c500" in ref_runs and not args.no_accuracy:
+        for name, prec in (("fp64", pkg.FP64), ("split", pkg.SPLIT)):
+            if name == "split" and args.no_split:
+                continue
+            accuracy[name] = accuracy_vs_reference(pkg, prec, mesh, ref_runs["s192_c500"])
 
     # ---- split precision on the same workload (config 2) ------------------
     split = None
@@ -489,19 +627,17 @@ def main():
         gs = pkg.Lulesh(args.size, pkg.INIT_V2, pkg.SPLIT)
         sms, slaunch = timed(gs, args.steps)
         svalue = world * ne * args.steps / (sms * 1e-3) * 1e-6
-        smetrics = pkg.sedov_metrics(gs, mesh)
         sroof, skernels, sbytes = kernel_table(gs, "split")
         gs.close()
         split = {"value": svalue, "unit": UNIT, "ms_per_step": sms / args.steps,
                  "speedup_vs_fp64": svalue / value, "gpu_launches": slaunch,
-                 "errors_vs_fp64": pkg.relative_errors(smetrics, ref_metrics),
-                 "compared_at_cycle": args.warmup + args.steps, "results": smetrics,
-                 "roofline": sroof, "kernels": skernels, "bytes_per_zone_cycle": sbytes,
+                 "errors_vs_reference": accuracy.get("split"),
+                 "roofline": sroof, "kernels": skernels, **sbytes,
                  "dtype": "f32 geometry/forces/Q, f64 state/EOS/volume/vdov/dt"}
 
     batched = None
     if args.precision == "fp64" and not args.no_batch:
-        batched = batch_legs(pkg, torch, args, barrier, max_over_ranks)
+        batched = batch_legs(pkg, torch, args, barrier, max_over_ranks, ref_runs)
 
     regions = None
     if args.precision == "fp64" and not args.no_regions:
@@ -521,13 +657,42 @@ def main():
                 "config": config_for(args, ne, nn), "roofline": roofline,
                 "fp64": {"peak_tflops_probe": fp64_peak, "pipe_rates_per_sm_clk": pkg.probe_pipe_rates(),
                          "note": "the FP64 pipe, not HBM, bounds this path: see roofline.fp64_issue"},
-                "bytes_per_zone_cycle": cycle_bytes,
+                **cycle_bytes,
                 "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clocks.summary(), "results": ref_metrics, "split": split,
+                "clocks": clocks.summary(), "accuracy_vs_reference": accuracy, "split": split,
                 "batched": batched, "regions": regions}
+        line["summary"] = summary_of(line)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def summary_of(line: dict) -> dict:
+    """The legs' headline figures, repeated last so a truncated line keeps them."""
+    out = {"fp64": round(line["value"], 1), "e2e": round(line["e2e"]["value"], 1),
+           "hbm_frac_K1": round(line["roofline"]["frac"], 4)}
+    acc = line.get("accuracy_vs_reference") or {}
+    if "fp64" in acc:
+        out["fp64_vs_reference"] = {"cycles_equal": acc["fp64"]["cycles_equal"],
+                                    "origin_energy": acc["fp64"]["errors"]["origin_energy"]}
+    sp = line.get("split")
+    if sp:
+        out["split"] = round(sp["value"], 1)
+        out["split_speedup"] = round(sp["speedup_vs_fp64"], 3)
+        if sp.get("errors_vs_reference"):
+            out["split_errors_vs_reference"] = sp["errors_vs_reference"]["errors"]
+    for name, leg in (line.get("batched") or {}).items():
+        out[name] = {"value": round(leg["value"], 1),
+                     "speedup_vs_one_at_a_time_fp64": round(leg["speedup_vs_one_at_a_time_fp64"], 3)}
+        if leg.get("origin_energy_error_vs_reference"):
+            e = leg["origin_energy_error_vs_reference"]
+            out[name]["origin_energy_error_max"] = e["max"]
+            out[name]["instances_compared"] = e["instances_compared"]
+    if line.get("regions"):
+        out["regions"] = round(line["regions"]["value"], 1)
+    if line.get("cpu_baseline"):
+        out["cpu_reference"] = round(line["cpu_baseline"]["value"], 2)
+    return out
 
 
 if __name__ == "__main__":
