@@ -6,20 +6,32 @@ s=192 mesh (7,077,888 elements, 7,189,057 nodes) with LULESH 2.0 initial
 conditions.  The headline metric is zone-cycles per second (elements x
 cycles / time), the reference's own figure of merit.
 
+The plain path (LULESH_PRECISION_FP64) keeps its state, node update, EOS and
+time constraints in FP64 and evaluates the element geometry and forces as
+double-float pairs on the FP32 pipe; the same workload with every operation
+in IEEE FP64 is the fp64_ieee leg.
+
 Legs of the default run (one JSON line on rank 0):
   value        K cycles through the captured run-loop graph, state resident
                in HBM; CUDA events on the library's stream
   roofline     per-kernel device time of a kernel-by-kernel pass (CUDA
-               events between launches) against the kernel's algorithmic
-               bytes; HBM peak from MEASURED_PEAKS.json
+               events between launches) against the step's algorithmic
+               bytes (K1/K2/K3); HBM peak from MEASURED_PEAKS.json; beside
+               it the FP64 and FP32 issue rooflines that bind
   e2e          the same cycles through the public C ABI with host buffers:
                upload of the state from pinned memory, one
                lulesh_time_increment + lulesh_lagrange_leapfrog call per cycle
-               with its status/scalar read-back, download of the final state
+               with its status/scalar read-back, download of the final state;
+               and a variant that copies the whole Domain every cycle
+  accuracy     500 cycles from the initial state in each arithmetic, against
+               the unmodified reference's own 500-cycle run
+  fp64_ieee    the same workload, every operation in IEEE FP64
   cpu_baseline the reference CPU implementation on this host's cores, a
                bounded sample of the same workload
   split        the same workload in split precision
   batched      the seeded ensembles (64 FP64 instances; 528 split instances)
+               against one-at-a-time runs and the reference's per-instance
+               answers
   regions      LULESH 2.0 material regions with EOS cost (-r 11 -b 1 -c 1) on
                the same mesh, beside the unmodified LULESH 2.0 program
 
@@ -439,6 +451,7 @@ def main():
                     help="cycles of the e2e variant that copies the whole Domain every cycle")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the 500-cycle runs compared with the reference's own")
+    ap.add_argument("--no-ieee", action="store_true", help="skip the all-IEEE-FP64 leg")
     ap.add_argument("--cpu-cycles", type=int, default=40,
                     help="cycles of the CPU baseline sample (about 10 s of the 16-core host at s=192)")
     ap.add_argument("--no-cpu", action="store_true")
@@ -502,10 +515,11 @@ def main():
         assert done == steps, (done, steps)
         return max_over_ranks(e0.elapsed_time(e1)), ctx.kernel_launches - l0
 
-    def kernel_table(ctx, precision):
+    def kernel_table(ctx, precision, traffic_key=None):
         """Per-kernel device time from a kernel-by-kernel pass, the roofline
         of the dominant kernel against the step's algorithmic bytes (K1, K2,
-        K3), and the bytes per zone-cycle."""
+        K3), and the bytes per zone-cycle.  traffic_key names the entry of
+        profiles/traffic.json measured for these kernels (default: precision)."""
         pc, kms = ctx.run_profiled(args.profile_cycles)
         per_launch = {k: v / max(pc, 1) for k, v in kms.items()}
         abytes = algorithmic_bytes(ne, nn, precision)
@@ -517,15 +531,15 @@ def main():
         achieved = sbytes[part] / (part_ms * 1e-3) * 1e-9
         design_achieved = abytes[top] / (per_launch[top] * 1e-3) * 1e-9
         traffic = None
-        fp64 = None
+        fp64 = fp32 = None
         tf = ROOT / "profiles" / "traffic.json"
         if tf.exists():
-            t = json.loads(tf.read_text()).get(precision, {}).get(top)
+            t = json.loads(tf.read_text()).get(traffic_key or precision, {}).get(top)
             if t:
                 traffic = t["bytes_per_elem"] * ne
+                units = nn if top == "node_update" else ne
+                secs = per_launch[top] * 1e-3
                 if "fp64_flops_per_unit" in t:
-                    units = nn if top == "node_update" else ne
-                    secs = per_launch[top] * 1e-3
                     ach = t["fp64_flops_per_unit"] * units / secs * 1e-12
                     # DADD and DMUL occupy an FP64 issue slot like a DFMA: the
                     # pipe's utilisation is instructions / (DFMA slots)
@@ -536,6 +550,16 @@ def main():
                             "issue_frac": inst_rate / slot_rate,
                             "peak_source": "measured FP64 FMA probe (lulesh_probe_fp64_peak)",
                             "flops_source": "per-unit FP64 work from the ncu capture in profiles/traffic.json"}
+                if "fp32_inst_per_unit" in t:
+                    # FP32 lane operations per second at the measured FFMA
+                    # issue rate, SM count and median clock of the timed run
+                    lane_rate = fp32_lanes_per_s()
+                    fp32 = {"bound": "fp32", "kernel": top,
+                            "achieved_ginst_per_s": t["fp32_inst_per_unit"] * units / secs * 1e-9,
+                            "peak_ginst_per_s": lane_rate * 1e-9,
+                            "issue_frac": t["fp32_inst_per_unit"] * units / secs / lane_rate,
+                            "peak_source": "measured FP32 FMA probe (lulesh_probe_pipe_rates) x SMs x clock",
+                            "inst_source": "per-unit FP32 instructions from the ncu capture in profiles/traffic.json"}
         roof = {"bound": "hbm", "kernel": top, "step_kernel": part, "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                 "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
@@ -543,7 +567,7 @@ def main():
                 "algorithmic_bytes_source": f"the step's {part} traffic (48/node gathered, 4-byte indices, "
                                             "8-byte doubles; FP32 corner forces in split precision)",
                 "design_bytes_per_launch": abytes[top], "design_achieved": design_achieved,
-                "design_frac": design_achieved / peaks["hbm_gbs"], "fp64_issue": fp64}
+                "design_frac": design_achieved / peaks["hbm_gbs"], "fp64_issue": fp64, "fp32_issue": fp32}
         total = sum(per_launch.values())
         table = {k: {"ms": per_launch[k], "share": per_launch[k] / total,
                      "design_gbs": abytes[k] / (per_launch[k] * 1e-3) * 1e-9 if per_launch[k] > 0 else 0.0}
@@ -557,10 +581,17 @@ def main():
 
     mesh = pkg.mesh_build(args.size, pkg.INIT_V2)
     fp64_peak = pkg.probe_fp64_peak()
+    pipe_rates = pkg.probe_pipe_rates()
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+
+    def fp32_lanes_per_s():
+        mhz = (clock_summary or {}).get("sm_mhz") or 2070.0
+        return pipe_rates["ffma"] * n_sm * mhz * 1e6
 
     # ---- plain FP64: K cycles through the run-loop graph -----------------
     clocks = ClockSampler(local)
     ms, launches = timed(g, args.steps, clocks)       # already the slowest rank's time
+    clock_summary = clocks.summary()
     value = world * ne * args.steps / (ms * 1e-3) * 1e-6
     roofline, kernels, cycle_bytes = kernel_table(g, args.precision)
 
@@ -616,10 +647,23 @@ def main():
     ref_runs = load_reference_runs()
     accuracy = {}
     if args.size == 192 and "s192_c500" in ref_runs and not args.no_accuracy:
-        for name, prec in (("fp64", pkg.FP64), ("split", pkg.SPLIT)):
-            if name == "split" and args.no_split:
+        for name, prec in (("fp64", pkg.FP64), ("fp64_ieee", pkg.FP64_IEEE), ("split", pkg.SPLIT)):
+            if (name == "split" and args.no_split) or (name == "fp64_ieee" and args.no_ieee):
                 continue
             accuracy[name] = accuracy_vs_reference(pkg, prec, mesh, ref_runs["s192_c500"])
+
+    # ---- every operation in IEEE FP64, same workload ------------------------
+    ieee = None
+    if args.precision == "fp64" and not args.no_ieee:
+        gi = pkg.Lulesh(args.size, pkg.INIT_V2, pkg.FP64_IEEE)
+        ims, ilaunch = timed(gi, args.steps)
+        ivalue = world * ne * args.steps / (ims * 1e-3) * 1e-6
+        iroof, ikernels, _ = kernel_table(gi, "fp64", "fp64_ieee")
+        gi.close()
+        ieee = {"value": ivalue, "unit": UNIT, "ms_per_step": ims / args.steps, "gpu_launches": ilaunch,
+                "value_over_ieee": value / ivalue, "errors_vs_reference": accuracy.get("fp64_ieee"),
+                "roofline": iroof, "kernels": ikernels,
+                "dtype": "f64: every operation IEEE FP64 (LULESH_PRECISION_FP64_IEEE)"}
 
     # ---- split precision on the same workload (config 2) ------------------
     split = None
@@ -654,12 +698,16 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "arithmetic": "FP64 state, node update, EOS and time constraints; element geometry and forces "
+                              "in double-float pairs of f32 (~48-bit significand) on the FP32 pipe, held to the "
+                              "FP64 parity bar (fp64_ieee: every operation IEEE FP64)",
                 "config": config_for(args, ne, nn), "roofline": roofline,
-                "fp64": {"peak_tflops_probe": fp64_peak, "pipe_rates_per_sm_clk": pkg.probe_pipe_rates(),
-                         "note": "the FP64 pipe, not HBM, bounds this path: see roofline.fp64_issue"},
+                "fp64": {"peak_tflops_probe": fp64_peak, "pipe_rates_per_sm_clk": pipe_rates,
+                         "note": "the FP64 and FP32 pipes, not HBM, bound this path: see roofline.fp64_issue "
+                                 "and roofline.fp32_issue"},
                 **cycle_bytes,
                 "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clocks.summary(), "accuracy_vs_reference": accuracy, "split": split,
+                "clocks": clock_summary, "accuracy_vs_reference": accuracy, "fp64_ieee": ieee, "split": split,
                 "batched": batched, "regions": regions}
         line["summary"] = summary_of(line)
         print(json.dumps(line), flush=True)
@@ -675,6 +723,11 @@ def summary_of(line: dict) -> dict:
     if "fp64" in acc:
         out["fp64_vs_reference"] = {"cycles_equal": acc["fp64"]["cycles_equal"],
                                     "origin_energy": acc["fp64"]["errors"]["origin_energy"]}
+    if line.get("fp64_ieee"):
+        out["fp64_ieee"] = round(line["fp64_ieee"]["value"], 1)
+        if "fp64_ieee" in acc:
+            out["fp64_ieee_vs_reference"] = {"cycles_equal": acc["fp64_ieee"]["cycles_equal"],
+                                             "origin_energy": acc["fp64_ieee"]["errors"]["origin_energy"]}
     sp = line.get("split")
     if sp:
         out["split"] = round(sp["value"], 1)

@@ -44,8 +44,13 @@ extern "C" {
 #define LULESH_ERR_ARG      (-5)   /* bad argument */
 
 /* ---- precision of the element kernels -------------------------------- */
-#define LULESH_PRECISION_FP64  0   /* plain FP64, the drop-in */
-#define LULESH_PRECISION_SPLIT 1   /* FP32 geometry/forces/Q gradients, FP64 state */
+#define LULESH_PRECISION_FP64      0   /* plain FP64, the drop-in: FP64 state, node
+                                          update, EOS and time constraints; element
+                                          geometry and forces in double-float (pairs
+                                          of FP32, ~48-bit significand) on the FP32
+                                          pipe, held to the FP64 parity bar */
+#define LULESH_PRECISION_SPLIT     1   /* FP32 geometry/forces/Q gradients, FP64 state */
+#define LULESH_PRECISION_FP64_IEEE 2   /* every operation in IEEE FP64 */
 
 /* ---- initial conditions of the Sedov problem ------------------------- */
 #define LULESH_INIT_V1 1           /* e(0)=3.948746e7, dt0=1e-7 (LULESH-OMP.cc:3053,3112) */

@@ -39,7 +39,7 @@ _PKG = Path(__file__).resolve().parent
 LIB_NAME = "liblulesh_gb300.so"
 
 OK, VOLUME_ERROR, QSTOP_ERROR, ERR_CUDA, ERR_TIMEOUT, ERR_ARG = 0, -1, -2, -3, -4, -5
-FP64, SPLIT = 0, 1
+FP64, SPLIT, FP64_IEEE = 0, 1, 2
 RUN_CYCLE_BUDGET = 1 << 20   # LULESH_RUN_CYCLE_BUDGET: cycles of a run given no cap
 INIT_V1, INIT_V2 = 1, 2
 

@@ -23,7 +23,8 @@ DRIVER = PKG / "lulesh_gb300_main"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
            "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", str(PKG.parent / "include")]
-SOURCES = ["api.cu", "step_fp64.cu", "step_split.cu", "batch.cu", "mesh.cpp", "noalloc.cu", "output.cpp"]
+SOURCES = ["api.cu", "step_fp64.cu", "step_df.cu", "step_split.cu", "batch.cu", "mesh.cpp", "noalloc.cu",
+           "output.cpp"]
 
 
 def nvcc() -> str:

@@ -378,7 +378,8 @@ int create_from_mesh(const HostMesh &m, int precision, const lulesh_params *para
     A(d.vnew, ne); A(d.delv, ne); A(d.vdov, ne); A(d.arealg, ne); A(d.ql, ne); A(d.qq, ne);
     A(d.delv_xi, ne); A(d.delv_eta, ne); A(d.delv_zeta, ne);
     A(d.delx_xi, ne); A(d.delx_eta, ne); A(d.delx_zeta, ne);
-    if (precision == LULESH_PRECISION_FP64) {
+    d.df = arith_of(precision);
+    if (precision != LULESH_PRECISION_SPLIT) {
         A(d.fcx, 8 * ne); A(d.fcy, 8 * ne); A(d.fcz, 8 * ne);
         A(d.geo, (size_t)kGeoWords * ne);
     } else {
@@ -459,7 +460,8 @@ int create_from_mesh(const HostMesh &m, int precision, const lulesh_params *para
 
 int check_precision(int precision, const char *who)
 {
-    if (precision != LULESH_PRECISION_FP64 && precision != LULESH_PRECISION_SPLIT)
+    if (precision != LULESH_PRECISION_FP64 && precision != LULESH_PRECISION_SPLIT &&
+        precision != LULESH_PRECISION_FP64_IEEE)
         return fail(nullptr, LULESH_ERR_ARG, std::string(who) + ": unknown precision");
     return LULESH_OK;
 }

@@ -111,7 +111,7 @@ int balloc(lulesh_batch *b, T **p, size_t n)
 // one another once the small instances had retired.
 int size_class(int s, int precision)
 {
-    if (precision == LULESH_PRECISION_FP64) return 0;
+    if (precision != LULESH_PRECISION_SPLIT) return 0;
     return s <= 24 ? 0 : (s <= 48 ? 1 : 2);
 }
 
@@ -224,7 +224,7 @@ void launch_kernel(lulesh_batch *b, int kernel, int cls, cudaStream_t st)
 int max_blocks(lulesh_batch *b, int kernel, int block)
 {
     return b->precision == LULESH_PRECISION_SPLIT ? batch_max_blocks_split(kernel, block)
-                                                  : batch_max_blocks_fp64(kernel, block);
+                                                  : batch_max_blocks_fp64(kernel, block, b->dom.df);
 }
 
 unsigned compact_blocks(const lulesh_batch *b)
@@ -352,7 +352,7 @@ std::string tune_key(const lulesh_batch *b, int cls, int kernel)
     cudaGetDeviceProperties(&prop, dev);
     std::ostringstream o;
     o << prop.name << "|sm" << prop.multiProcessorCount << "|"
-      << (b->precision == LULESH_PRECISION_SPLIT ? "split" : "fp64") << "|class" << cls << "|"
+      << (b->precision == LULESH_PRECISION_SPLIT ? "split" : (b->dom.df == kArithDF64 ? "fp64" : "fp64ieee")) << "|class" << cls << "|"
       << kKernelNames[kernel];
     return o.str();
 }
@@ -424,7 +424,8 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
     if (!out || n < 1 || !sizes) return bfail(nullptr, LULESH_ERR_ARG, "lulesh_batch_create: bad arguments");
     if (init_mode != LULESH_INIT_V1 && init_mode != LULESH_INIT_V2)
         return bfail(nullptr, LULESH_ERR_ARG, "lulesh_batch_create: bad init_mode");
-    if (precision != LULESH_PRECISION_FP64 && precision != LULESH_PRECISION_SPLIT)
+    if (precision != LULESH_PRECISION_FP64 && precision != LULESH_PRECISION_SPLIT &&
+        precision != LULESH_PRECISION_FP64_IEEE)
         return bfail(nullptr, LULESH_ERR_ARG, "lulesh_batch_create: bad precision");
     long ne_sum = 0;
     for (int i = 0; i < n; ++i) {
@@ -517,7 +518,8 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
     A(d.vnew, ne); A(d.delv, ne); A(d.vdov, ne); A(d.arealg, ne);
     A(d.delv_xi, ne); A(d.delv_eta, ne); A(d.delv_zeta, ne);
     A(d.delx_xi, ne); A(d.delx_eta, ne); A(d.delx_zeta, ne);
-    if (precision == LULESH_PRECISION_FP64) {
+    d.df = arith_of(precision);
+    if (precision != LULESH_PRECISION_SPLIT) {
         A(d.fcx, 8 * ne); A(d.fcy, 8 * ne); A(d.fcz, 8 * ne);
         A(d.geo, (size_t)kGeoWords * ne);
     } else {

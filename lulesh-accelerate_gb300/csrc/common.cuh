@@ -3,6 +3,7 @@
 
 #include "lulesh_internal.h"
 #include "fastmath.cuh"
+#include "df64.cuh"
 
 #include <cuda_runtime.h>
 
@@ -137,15 +138,38 @@ __device__ __forceinline__ float d2f(double v)
 }
 
 // float -> double, exact (FP32 subnormals become zeros).
-__device__ __forceinline__ double f2d(float f)
+__device__ __forceinline__ double f2d(float f) { return df_f2d(f); }
+
+// The node update after the corner gather: CalcAccelerationForNodes, the
+// symmetry-plane conditions, CalcVelocityForNodes and CalcPositionForNodes
+// (LULESH-OMP.cc:1613-1683) for node n with nodal force (fx, fy, fz).
+__device__ __forceinline__ void node_integrate(const Dom &d, int n, const DevScalars *sc, double fx, double fy,
+                                               double fz)
 {
-    const unsigned u = __float_as_uint(f);
-    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
-    const unsigned fe = (u >> 23) & 0xffu;
-    const unsigned long long mant = (unsigned long long)(u & 0x7fffffu) << 29;
-    if (fe == 0) return __longlong_as_double((long long)sign);
-    const unsigned long long de = (fe == 0xff) ? 0x7ffULL : (unsigned long long)(fe - 127 + 1023);
-    return __longlong_as_double((long long)(sign | (de << 52) | mant));
+    if (d.keep & 1) {
+        d.fx[n] = fx;
+        d.fy[n] = fy;
+        d.fz[n] = fz;
+    }
+    const double dt = sc->deltatime, u_cut = d.prm.u_cut;
+    const unsigned bc = __ldg(d.node_bc + n);
+    double ax, ay, az;
+    if (d.inv_mass) {
+        // f * (1/m) with the reciprocal precomputed: within an ulp of f / m
+        const double im = __ldg(d.inv_mass + n);
+        ax = (bc & 1) ? 0.0 : fx * im;
+        ay = (bc & 2) ? 0.0 : fy * im;
+        az = (bc & 4) ? 0.0 : fz * im;
+    } else {
+        const double m = __ldg(d.nodal_mass + n);
+        ax = (bc & 1) ? 0.0 : fx / m;
+        ay = (bc & 2) ? 0.0 : fy / m;
+        az = (bc & 4) ? 0.0 : fz / m;
+    }
+    double t;
+    t = d.xd[n] + ax * dt; if (abs_lt(t, u_cut)) t = 0.0; d.xd[n] = t; d.x[n] += t * dt;
+    t = d.yd[n] + ay * dt; if (abs_lt(t, u_cut)) t = 0.0; d.yd[n] = t; d.y[n] += t * dt;
+    t = d.zd[n] + az * dt; if (abs_lt(t, u_cut)) t = 0.0; d.zd[n] = t; d.z[n] += t * dt;
 }
 
 // One direction of the monotonic limiter (:2198-2228).

@@ -26,6 +26,9 @@
 #pragma once
 
 #include "fastmath.cuh"
+#include "df64.cuh"
+
+#include <type_traits>
 
 namespace lulesh {
 
@@ -157,15 +160,14 @@ __device__ __forceinline__ ModeCrosses<T> mode_crosses(const V3<T> &M1, const V3
 // coefficients are taken three times over (3 W1 = 3 M2xM3 + M4xM5,
 // 3 W4 = M2xM6 + M5xM1, ...) so that no multiplication by 1/3 is needed.
 template <typename T>
-__device__ __forceinline__ void force_geometry(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
-                                               const V3<T> &M4, const V3<T> &M5, const V3<T> &M6,
-                                               const ModeCrosses<T> &C, T dx[8], T dy[8], T dz[8], V3<T> nx[3])
+__device__ __forceinline__ void volume_derivative(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
+                                                  const V3<T> &M4, const V3<T> &M5, const V3<T> &M6,
+                                                  const ModeCrosses<T> &C, T dx[8], T dy[8], T dz[8])
 {
     const V3<T> &c23 = C.c23, &c45 = C.c45, &c31 = C.c31, &c64 = C.c64, &c12 = C.c12, &c56 = C.c56;
     auto add3 = [](const V3<T> &a, T s, const V3<T> &b) {
         return V3<T>{a.x * s + b.x, a.y * s + b.y, a.z * s + b.z};
     };
-    auto sum3 = [](const V3<T> &a, const V3<T> &b) { return V3<T>{a.x + b.x, a.y + b.y, a.z + b.z}; };
     const V3<T> W1 = add3(c23, T(3.0), c45);
     const V3<T> W2 = add3(c31, T(3.0), c64);
     const V3<T> W3 = add3(c12, T(3.0), c56);
@@ -175,10 +177,24 @@ __device__ __forceinline__ void force_geometry(const V3<T> &M1, const V3<T> &M2,
     inv_walsh6(W1.x, W2.x, W3.x, W4.x, W5.x, W6.x, dx);
     inv_walsh6(W1.y, W2.y, W3.y, W4.y, W5.y, W6.y, dy);
     inv_walsh6(W1.z, W2.z, W3.z, W4.z, W5.z, W6.z, dz);
+}
 
-    nx[0] = sum3(c23, c45);
-    nx[1] = sum3(c31, c64);
-    nx[2] = sum3(c12, c56);
+template <typename T>
+__device__ __forceinline__ void normal_generators(const ModeCrosses<T> &C, V3<T> nx[3])
+{
+    auto sum3 = [](const V3<T> &a, const V3<T> &b) { return V3<T>{a.x + b.x, a.y + b.y, a.z + b.z}; };
+    nx[0] = sum3(C.c23, C.c45);
+    nx[1] = sum3(C.c31, C.c64);
+    nx[2] = sum3(C.c12, C.c56);
+}
+
+template <typename T>
+__device__ __forceinline__ void force_geometry(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
+                                               const V3<T> &M4, const V3<T> &M5, const V3<T> &M6,
+                                               const ModeCrosses<T> &C, T dx[8], T dy[8], T dz[8], V3<T> nx[3])
+{
+    volume_derivative(M1, M2, M3, M4, M5, M6, C, dx, dy, dz);
+    normal_generators(C, nx);
 }
 
 // 64 x volume through the shared crosses: the bilinear terms of the volume formula above are
@@ -187,7 +203,7 @@ template <typename T>
 __device__ __forceinline__ T volume64_shared(const V3<T> &M1, const V3<T> &M2, const V3<T> &M3,
                                              const ModeCrosses<T> &C)
 {
-    const T third = T(1.0) / T(3.0);
+    const T third = T(1.0 / 3.0);
     return fma(dot3_acc(M1, C.c45, dot3_acc(M3, C.c56, dot3(M2, C.c64))), third, dot3(M1, C.c23));
 }
 
@@ -212,7 +228,7 @@ __device__ __forceinline__ T max_face_cross2_64(const V3<T> &M1, const V3<T> &M2
     const T f1 = pair(C.c23, C.c45, b, a, T(-1.0));   // Y1 = b - a
     const T f2 = pair(C.c31, C.c64, c, a, T(1.0));    // Y2 = c + a
     const T f3 = pair(C.c12, C.c56, c, b, T(1.0));    // |Y3| = |c + b|
-    if constexpr (sizeof(T) == 8) {
+    if constexpr (std::is_same<T, double>::value) {
         // the three are >= 0, so their bit patterns order like the values:
         // compare those on the integer pipes instead of two FP64 max slots
         unsigned long long k1, k2, k3;

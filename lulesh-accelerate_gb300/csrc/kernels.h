@@ -48,6 +48,14 @@ void launch_rate_probe(int which, float *out, int blocks, int threads, int iters
 // library's inverse cube root and square root from CUDA's, over n arguments
 void launch_math_probe(unsigned long long *keys, int n, cudaStream_t st);
 
+// The plain path's double-float element kernels (step_df.cu); the launchers
+// above call them when Dom::df is set.
+void launch_elem_force_df(const Dom &d, cudaStream_t st);
+void launch_node_update_df(const Dom &d, cudaStream_t st);
+void launch_elem_kinematics_df(const Dom &d, cudaStream_t st);
+void launch_batch_kernel_df(const Dom &d, const BatchView &b, cudaStream_t st, int kernel, int cls, LaunchCfg cfg);
+int batch_max_blocks_df(int kernel, int block);
+
 // Split-precision path (step_split.cu).
 void launch_split_sync(const Dom &d, cudaStream_t st);
 void launch_lagrange_nodal_split(const Dom &d, cudaStream_t st);
@@ -61,7 +69,7 @@ void launch_batch_kernel_fp64(const Dom &d, const BatchView &b, cudaStream_t st,
                               LaunchCfg cfg);
 void launch_batch_kernel_split(const Dom &d, const BatchView &b, cudaStream_t st, int kernel, int cls,
                                LaunchCfg cfg);
-int batch_max_blocks_fp64(int kernel, int block);
+int batch_max_blocks_fp64(int kernel, int block, int arith);
 int batch_max_blocks_split(int kernel, int block);
 
 }  // namespace lulesh

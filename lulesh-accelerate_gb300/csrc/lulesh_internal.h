@@ -88,6 +88,18 @@ int write_domain_file(const char *basename, int s, long ne, long nn, const int *
 void set_last_error(const std::string &msg);
 void default_params(lulesh_params *p);
 
+// Arithmetic of the kernels of a context whose state is FP64 (Dom::df):
+//   kArithDF64   element geometry and forces in double-float pairs on the
+//                FP32 pipe (step_df.cu; LULESH_PRECISION_FP64), corner forces
+//                and the geometry cache stored as float2 pairs
+//   kArithIEEE   every operation in IEEE FP64 (step_fp64.cu's element
+//                kernels; LULESH_PRECISION_FP64_IEEE)
+enum : int { kArithIEEE = 0, kArithDF64 = 1 };
+inline int arith_of(int precision)
+{
+    return precision == LULESH_PRECISION_FP64 ? kArithDF64 : kArithIEEE;
+}
+
 // Everything one kernel launch needs, passed by value.
 // Words per element of the FP64 path's geometry cache (Dom::geo).
 constexpr int kGeoWords = 39;
@@ -108,6 +120,8 @@ struct Dom {
     // kBlockNode); smaller on small meshes so that the blocks spread over
     // every SM
     int eblock, nblock;
+    // arithmetic of the FP64-state kernels (kArith*; arith_of)
+    int df;
     const double *volo, *elem_mass, *nodal_mass;
     // nodal state
     double *x, *y, *z, *xd, *yd, *zd;
@@ -133,7 +147,9 @@ struct Dom {
     // kinematics kernel for the next cycle's force kernel (the positions do
     // not change between the two): the Walsh modes M1..M7 (21 words) and the
     // six shared cross products (18 words), [kGeoWords][ne]; valid while
-    // DevScalars::geo_valid is set.  Null: not kept.
+    // DevScalars::geo_valid is set.  Null: not kept.  With df set each word
+    // is a double-float pair (float2) instead of a double, and so are the
+    // corner forces fcx/fcy/fcz.
     double *geo;
     float *gq;
     DevScalars *sc;

@@ -179,6 +179,7 @@ extern "C" int lulesh_lagrange_nodal_noalloc(
     d.ne = num_elem;
     d.nn = num_node;
     d.keep = keep ? 1 : 0;
+    d.df = arith_of(LULESH_PRECISION_FP64);   // the plain path's arithmetic
     d.nodelist = nodelist;
     d.corner_start = reinterpret_cast<const int *>(base + kOffStart);
     d.corner_list = reinterpret_cast<const int *>(base + kOffSlots);

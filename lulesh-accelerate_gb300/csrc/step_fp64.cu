@@ -250,30 +250,7 @@ __device__ __forceinline__ void node_update_fp64(const Dom &d, int n, const DevS
         fy += d.fcy[c];
         fz += d.fcz[c];
     }
-    if (d.keep & 1) {
-        d.fx[n] = fx;
-        d.fy[n] = fy;
-        d.fz[n] = fz;
-    }
-    const double dt = sc->deltatime, u_cut = d.prm.u_cut;
-    const unsigned bc = __ldg(d.node_bc + n);
-    double ax, ay, az;
-    if (d.inv_mass) {
-        // f * (1/m) with the reciprocal precomputed: within an ulp of f / m
-        const double im = __ldg(d.inv_mass + n);
-        ax = (bc & 1) ? 0.0 : fx * im;
-        ay = (bc & 2) ? 0.0 : fy * im;
-        az = (bc & 4) ? 0.0 : fz * im;
-    } else {
-        const double m = __ldg(d.nodal_mass + n);
-        ax = (bc & 1) ? 0.0 : fx / m;
-        ay = (bc & 2) ? 0.0 : fy / m;
-        az = (bc & 4) ? 0.0 : fz / m;
-    }
-    double t;
-    t = d.xd[n] + ax * dt; if (abs_lt(t, u_cut)) t = 0.0; d.xd[n] = t; d.x[n] += t * dt;
-    t = d.yd[n] + ay * dt; if (abs_lt(t, u_cut)) t = 0.0; d.yd[n] = t; d.y[n] += t * dt;
-    t = d.zd[n] + az * dt; if (abs_lt(t, u_cut)) t = 0.0; d.zd[n] = t; d.z[n] += t * dt;
+    node_integrate(d, n, sc, fx, fy, fz);
 }
 
 __global__ void __launch_bounds__(kBlockNode) k_node_update(const __grid_constant__ Dom d)
@@ -479,15 +456,35 @@ void launch_time_increment(const Dom &d, cudaStream_t st)
     k_time_increment<<<1, 1, 0, st>>>(d);
 }
 
+// Dom::df: kArithDF64 the element geometry and forces in double-float
+// (step_df.cu), kArithIEEE every operation in FP64 (this file's kernels)
+static void launch_elem_force(const Dom &d, cudaStream_t st)
+{
+    if (d.df == kArithDF64) launch_elem_force_df(d, st);
+    else k_elem_force<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+}
+
+static void launch_node_update(const Dom &d, cudaStream_t st)
+{
+    if (d.df == kArithDF64) launch_node_update_df(d, st);
+    else k_node_update<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
+}
+
+static void launch_elem_kinematics(const Dom &d, cudaStream_t st)
+{
+    if (d.df == kArithDF64) launch_elem_kinematics_df(d, st);
+    else k_elem_kinematics<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+}
+
 void launch_lagrange_nodal(const Dom &d, cudaStream_t st)
 {
-    k_elem_force<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
-    k_node_update<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
+    launch_elem_force(d, st);
+    launch_node_update(d, st);
 }
 
 void launch_lagrange_elements(const Dom &d, cudaStream_t st, bool with_constraints)
 {
-    k_elem_kinematics<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    launch_elem_kinematics(d, st);
     if (with_constraints)
         k_elem_material<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     else
@@ -536,11 +533,11 @@ void launch_cycle_timed(const Dom &d, cudaStream_t st, cudaEvent_t ev[7])
     cudaEventRecord(ev[0], st);
     k_time_increment<<<1, 1, 0, st>>>(d);
     cudaEventRecord(ev[1], st);
-    k_elem_force<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    launch_elem_force(d, st);
     cudaEventRecord(ev[2], st);
-    k_node_update<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
+    launch_node_update(d, st);
     cudaEventRecord(ev[3], st);
-    k_elem_kinematics<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    launch_elem_kinematics(d, st);
     cudaEventRecord(ev[4], st);
     k_elem_material<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     cudaEventRecord(ev[5], st);
@@ -658,6 +655,10 @@ void launch_rate_probe(int which, float *out, int blocks, int threads, int iters
 void launch_batch_kernel_fp64(const Dom &d, const BatchView &b, cudaStream_t st, int kernel, int cls,
                               LaunchCfg cfg)
 {
+    if (d.df == kArithDF64 && kernel < 3) {
+        launch_batch_kernel_df(d, b, st, kernel, cls, cfg);
+        return;
+    }
     switch (kernel) {
     case 0: kb_elem<elem_force_fp64><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     case 1: kb_node<node_update_fp64><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
@@ -667,8 +668,9 @@ void launch_batch_kernel_fp64(const Dom &d, const BatchView &b, cudaStream_t st,
 }
 
 // Resident blocks per SM of a batched kernel at a block size.
-int batch_max_blocks_fp64(int kernel, int block)
+int batch_max_blocks_fp64(int kernel, int block, int arith)
 {
+    if (arith == kArithDF64 && kernel < 3) return batch_max_blocks_df(kernel, block);
     int n = 0;
     cudaError_t e;
     switch (kernel) {

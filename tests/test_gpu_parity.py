@@ -6,6 +6,11 @@ exactly, its final origin energy to <= 1e-10 relative and its plane-0
 symmetry test.  Per phase, fields agree to <= 1e-12 of the field's largest
 magnitude: the kernels keep the reference's association but nvcc fuses
 multiply-adds, which moves results by a few units in the last place.
+
+The phase and full-run tests run both arithmetics of the FP64-state path,
+with the same bars: the default, whose element geometry and forces are
+double-float pairs on the FP32 pipe (~48-bit significand), and every
+operation in IEEE FP64.
 """
 from __future__ import annotations
 
@@ -19,6 +24,11 @@ pytestmark = pytest.mark.gpu
 E0_TOL = 1e-10          # final origin energy, relative
 PHASE_TOL = 1e-12       # per-phase fields, relative to the field's max |value|
 SCALAR_TOL = 1e-13      # time-step scalars
+PLAIN = ["fp64", "fp64_ieee"]
+
+
+def _prec(pkg, name):
+    return {"fp64": pkg.FP64, "fp64_ieee": pkg.FP64_IEEE}[name]
 
 
 def _init(pkg, name):
@@ -36,10 +46,11 @@ def _upload_stage(g, stage):
     g.scalars = sc
 
 
+@pytest.mark.parametrize("arith", PLAIN)
 @pytest.mark.parametrize("s,cyc", [(5, 0), (6, 40), (10, 150)])
-def test_phase_parity_with_reference(pkg, s, cyc):
+def test_phase_parity_with_reference(pkg, s, cyc, arith):
     st = load_phases(s, cyc)
-    with pkg.Lulesh(s, pkg.INIT_V2) as g:
+    with pkg.Lulesh(s, pkg.INIT_V2, _prec(pkg, arith)) as g:
         g.keep_forces(True)
         _upload_stage(g, st["start"])
         g.time_increment()
@@ -72,10 +83,11 @@ FULL_RUNS = [(1, "v1", 0), (2, "v1", 0), (3, "v1", 0), (1, "v2", 0), (2, "v2", 0
              (10, "v2", 0), (16, "v2", 0), (30, "v2", 0), (30, "v2", 100), (48, "v2", 40)]
 
 
+@pytest.mark.parametrize("arith", PLAIN)
 @pytest.mark.parametrize("s,init,cap", FULL_RUNS)
-def test_full_run_matches_reference(pkg, answers, s, init, cap):
+def test_full_run_matches_reference(pkg, answers, s, init, cap, arith):
     ref = find_run(answers, s, init, cap)
-    with pkg.Lulesh(s, _init(pkg, init)) as g:
+    with pkg.Lulesh(s, _init(pkg, init), _prec(pkg, arith)) as g:
         n = g.run(cap)
         sc = g.scalars
         assert n == ref["cycles"]
