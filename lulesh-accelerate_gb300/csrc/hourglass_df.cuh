@@ -44,13 +44,16 @@ __device__ __forceinline__ void fb_hourglass_df(const Dom &d, const int nl[8], c
         for (int c = 0; c < 8; ++c)
             hg[c][m] = fma(dvdz[c], hz, fma(dvdy[c], hy, fma(dvdx[c], hx, df64(gam[m][c], 0.f))));
     }
-    const double *vel[3] = {d.xd, d.yd, d.zd};
-#pragma unroll
+    // One velocity component per iteration, the loop kept rolled: the body is
+    // the same code three times over, and the smaller instruction footprint
+    // ran the force kernel 5 % faster at s=192 (2.09 -> 1.99 ms).
+#pragma unroll 1
     for (int dim = 0; dim < 3; ++dim) {
+        const double *vel = dim == 0 ? d.xd : (dim == 1 ? d.yd : d.zd);
         df64 u[8];
         {
             double ud[8];
-            gather8(vel[dim], nl, ud);
+            gather8(vel, nl, ud);
 #pragma unroll
             for (int c = 0; c < 8; ++c) u[c] = to_df(ud[c]);
         }

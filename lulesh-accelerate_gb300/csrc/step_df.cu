@@ -145,8 +145,12 @@ __device__ __forceinline__ void elem_force_df(const Dom &d, int k, DevScalars *s
         }
         if (dot3(M2, X.c31).hi <= 0.f) flag_error(sc, ERR_K1_DETERM, k);
     }
+    // (dim may be a run-time value: the component is selected, not indexed,
+    // so that Y stays in registers)
+    auto comp = [&](int i, int dim) { return dim == 0 ? Y[i][0] : (dim == 1 ? Y[i][1] : Y[i][2]); };
     auto stress8 = [&](int dim, df64 f[8]) {
-        const df64 a = Y[0][dim] + Y[1][dim], b = Y[0][dim] - Y[1][dim], z = Y[2][dim];
+        const df64 y0 = comp(0, dim), y1 = comp(1, dim);
+        const df64 a = y0 + y1, b = y0 - y1, z = comp(2, dim);
         f[0] = -(a + z);   // (-,-,-)
         f[1] = b - z;      // (+,-,-)
         f[2] = a - z;      // (+,+,-)
@@ -156,8 +160,9 @@ __device__ __forceinline__ void elem_force_df(const Dom &d, int k, DevScalars *s
         f[6] = -f[0];
         f[7] = -f[1];
     };
-    float2 *out[3] = {reinterpret_cast<float2 *>(d.fcx), reinterpret_cast<float2 *>(d.fcy),
-                      reinterpret_cast<float2 *>(d.fcz)};
+    auto out_of = [&](int dim) {
+        return reinterpret_cast<float2 *>(dim == 0 ? d.fcx : (dim == 1 ? d.fcy : d.fcz));
+    };
 
     // CalcHourglassControlForElems (:1503-1558)
     const double vk = d.v[k];
@@ -171,7 +176,7 @@ __device__ __forceinline__ void elem_force_df(const Dom &d, int k, DevScalars *s
             df64 f[8];
             stress8(dim, f);
 #pragma unroll
-            for (int c = 0; c < 8; ++c) out[dim][c * ne + k] = as_float2(f[c]);
+            for (int c = 0; c < 8; ++c) out_of(dim)[c * ne + k] = as_float2(f[c]);
         }
         return;
     }
@@ -186,7 +191,7 @@ __device__ __forceinline__ void elem_force_df(const Dom &d, int k, DevScalars *s
                         df64 f[8];
                         stress8(dim, f);
 #pragma unroll
-                        for (int c = 0; c < 8; ++c) out[dim][c * ne + k] = as_float2(f[c] + hgf[c]);
+                        for (int c = 0; c < 8; ++c) out_of(dim)[c * ne + k] = as_float2(f[c] + hgf[c]);
                     });
 }
 
