@@ -418,6 +418,24 @@ __device__ __forceinline__ void constraint_keys(double ss, double vdov, double a
     }
 }
 
+// The same candidates with the arithmetic in double-float pairs (the
+// default plain path): the comparisons that decide which terms enter stay
+// on the FP64 values.
+__device__ __forceinline__ void constraint_keys_df(double ss, double vdov, double arealg,
+                                                   const lulesh_params &P,
+                                                   unsigned long long &kc, unsigned long long &kh)
+{
+    kc = ~0ULL;
+    kh = ~0ULL;
+    if (iabs(vdov) != 0ULL) {
+        const df64 s = to_df(ss), a = to_df(arealg), v = to_df(vdov);
+        df64 dtf = s * s;
+        if (lt(vdov, 0.)) dtf = fma(to_df(64.0 * P.qqc * P.qqc) * (a * a), v * v, dtf);
+        kc = order_key(to_double(a * df_rsqrt(dtf)));          // arealg / sqrt(dtf)
+        kh = order_key(to_double(df_div(to_df(P.dvovmax), fabs(v) + df64(1.e-20))));
+    }
+}
+
 // Publish the constraint minima: a value is registered only when some
 // element was active and it is below the 1e20 start value (:2869-2871,
 // :2928-2930); otherwise the previous dtcourant/dthydro stay.

@@ -53,6 +53,7 @@ void launch_math_probe(unsigned long long *keys, int n, cudaStream_t st);
 void launch_elem_force_df(const Dom &d, cudaStream_t st);
 void launch_node_update_df(const Dom &d, cudaStream_t st);
 void launch_elem_kinematics_df(const Dom &d, cudaStream_t st);
+void launch_elem_material_df(const Dom &d, cudaStream_t st, bool with_constraints);
 void launch_batch_kernel_df(const Dom &d, const BatchView &b, cudaStream_t st, int kernel, int cls, LaunchCfg cfg);
 int batch_max_blocks_df(int kernel, int block);
 

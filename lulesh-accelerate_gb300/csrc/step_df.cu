@@ -31,6 +31,7 @@
 #include "hexmodes.cuh"
 #include "common.cuh"
 #include "hourglass_df.cuh"
+#include "eos_df.cuh"
 #include "batch_kernels.cuh"
 
 #include <cuda_runtime.h>
@@ -300,6 +301,109 @@ __global__ void __launch_bounds__(kBlockElem) k_elem_kinematics_df(const __grid_
 }
 
 // ---------------------------------------------------------------------
+// Monotonic-Q limiter and viscosity coefficients as pairs, then the FP64
+// material update, volume update and constraint candidates
+// ---------------------------------------------------------------------
+
+// One direction of the monotonic limiter (LULESH-OMP.cc:2198-2228) as
+// pairs.  The neighbour slopes are divided by the element's own (plus
+// 1e-36): in FP64 a vanishing own slope makes the ratios huge but finite,
+// and the clamp to [0, max_slope] absorbs them; in pairs the product would
+// overflow (and its remainder turn into a NaN), so a ratio whose magnitude
+// exceeds 2^100 -- judged from the high words before multiplying -- is
+// taken as +-2^100.  That changes no outcome: a ratio beyond it is never the
+// minimum unless both are, and then the result is max_slope either way; a
+// negative one makes the result 0 either way.
+__device__ __forceinline__ df64 limiter_phi_df(const double *__restrict__ delv, int i, int bm, int bp,
+                                               int m_symm, int m_free, int p_symm, int p_free, int lm, int lp,
+                                               df64 limiter, df64 max_slope)
+{
+    const double own = delv[i];
+    const df64 norm = df_rcp(to_df(own) + df64(1.e-36));
+    double dm = 0.0, dp = 0.0;
+    if (bm == 0) dm = delv[lm];
+    else if (bm == m_symm) dm = own;
+    if (bp == 0) dp = delv[lp];
+    else if (bp == p_symm) dp = own;
+    (void)m_free;
+    (void)p_free;
+    const float big = 1.2676506e30f;   // 2^100
+    auto ratio = [&](double x) {
+        const df64 a = to_df(x);
+        if (fabsf(a.hi) * fabsf(norm.hi) > big)   // may be inf: still > big
+            return (a.hi < 0.f) != (norm.hi < 0.f) ? df64(-big, 0.f) : df64(big, 0.f);
+        return a * norm;
+    };
+    df64 delvm = ratio(dm), delvp = ratio(dp);
+    df64 phi = df_scale(delvm + delvp, 0.5f);
+    delvm = delvm * limiter;
+    delvp = delvp * limiter;
+    if (df_gt(phi, delvm)) phi = delvm;
+    if (df_gt(phi, delvp)) phi = delvp;
+    if (phi.hi < 0.f) phi = df64(0.f, 0.f);
+    if (df_gt(phi, max_slope)) phi = max_slope;
+    return phi;
+}
+
+// Monotonic-Q region (:2182-2320) and the material update as pairs (the
+// energy accumulated in FP64), and the element's constraint keys in pairs
+// when kConstraints.
+template <bool kConstraints>
+__device__ __forceinline__ void elem_material_df(const Dom &d, int k, DevScalars *sc, unsigned long long &kc,
+                                                 unsigned long long &kh)
+{
+    const lulesh_params &P = d.prm;
+    const int bc = __ldg(d.elem_bc + k);
+    const df64 lim = to_df(P.monoq_limiter_mult), maxs = to_df(P.monoq_max_slope);
+    const df64 phixi = limiter_phi_df(d.delv_xi, k, bc & BC_XI_M, bc & BC_XI_P, BC_XI_M_SYMM, BC_XI_M_FREE,
+                                      BC_XI_P_SYMM, BC_XI_P_FREE, __ldg(d.lxim + k), __ldg(d.lxip + k), lim, maxs);
+    const df64 phieta = limiter_phi_df(d.delv_eta, k, bc & BC_ETA_M, bc & BC_ETA_P, BC_ETA_M_SYMM, BC_ETA_M_FREE,
+                                       BC_ETA_P_SYMM, BC_ETA_P_FREE, __ldg(d.letam + k), __ldg(d.letap + k), lim,
+                                       maxs);
+    const df64 phizeta = limiter_phi_df(d.delv_zeta, k, bc & BC_ZETA_M, bc & BC_ZETA_P, BC_ZETA_M_SYMM,
+                                        BC_ZETA_M_FREE, BC_ZETA_P_SYMM, BC_ZETA_P_FREE, __ldg(d.lzetam + k),
+                                        __ldg(d.lzetap + k), lim, maxs);
+    const double vnew = d.vnew[k], vdov = d.vdov[k];
+    df64 qlin(0.f, 0.f), qquad(0.f, 0.f);
+    if (!gt(vdov, 0.)) {
+        // the products delv * delx; a positive one contributes nothing
+        auto prod = [](double dv, double dx) {
+            const df64 p = to_df(dv) * to_df(dx);
+            return p.hi > 0.f ? df64(0.f, 0.f) : p;
+        };
+        const df64 dxi = prod(d.delv_xi[k], d.delx_xi[k]);
+        const df64 deta = prod(d.delv_eta[k], d.delx_eta[k]);
+        const df64 dzeta = prod(d.delv_zeta[k], d.delx_zeta[k]);
+        const df64 rho = df_div(to_df(d.elem_mass[k]), to_df(d.volo[k]) * to_df(vnew));
+        const df64 one(1.f, 0.f);
+        const df64 lin = (dxi * (one - phixi) + deta * (one - phieta)) + dzeta * (one - phizeta);
+        const df64 quad = (dxi * dxi * (one - phixi * phixi) + deta * deta * (one - phieta * phieta)) +
+                          dzeta * dzeta * (one - phizeta * phizeta);
+        qlin = -(to_df(P.qlc_monoq) * rho) * lin;
+        qquad = to_df(P.qqc_monoq) * rho * quad;
+    }
+    if (d.keep & 2) {
+        d.ql[k] = to_double(qlin);
+        d.qq[k] = to_double(qquad);
+    }
+    const double ssn = material_update_df(d, k, sc, vnew, qlin, qquad, d.reps ? __ldg(d.reps + k) : 1);
+    if (kConstraints) constraint_keys_df(ssn, vdov, d.arealg[k], P, kc, kh);
+}
+
+template <bool kConstraints>
+__global__ void __launch_bounds__(kBlockElem) k_elem_material_df(const __grid_constant__ Dom d)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long kc = ~0ULL, kh = ~0ULL;
+    if (t < d.ne && !skip_step(d)) {
+        // with regions, threads take elements in cost-grouped order
+        const int k = d.mat_order ? __ldg(d.mat_order + t) : t;
+        elem_material_df<kConstraints>(d, k, d.sc, kc, kh);
+    }
+    if (kConstraints) block_min_publish(kc, kh, d.sc);
+}
+
+// ---------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------
 static inline unsigned blocks_for(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -319,14 +423,23 @@ void launch_elem_kinematics_df(const Dom &d, cudaStream_t st)
     k_elem_kinematics_df<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
 }
 
-// Batched ensembles: kernels 0..2 (force, node update, kinematics) over the
-// active tiles of one class; the material kernel is step_fp64.cu's.
+void launch_elem_material_df(const Dom &d, cudaStream_t st, bool with_constraints)
+{
+    if (with_constraints)
+        k_elem_material_df<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    else
+        k_elem_material_df<false><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+}
+
+// Batched ensembles: kernels 0..3 (force, node update, kinematics, material)
+// over the active tiles of one class.
 void launch_batch_kernel_df(const Dom &d, const BatchView &b, cudaStream_t st, int kernel, int cls, LaunchCfg cfg)
 {
     switch (kernel) {
     case 0: kb_elem<elem_force_df><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     case 1: kb_node<node_update_df><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
-    default: kb_elem<elem_kinematics_df><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    case 2: kb_elem<elem_kinematics_df><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    default: kb_material<elem_material_df<true>><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     }
 }
 
@@ -337,7 +450,8 @@ int batch_max_blocks_df(int kernel, int block)
     switch (kernel) {
     case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_force_df>, block, 0); break;
     case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_node<node_update_df>, block, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_kinematics_df>, block, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_kinematics_df>, block, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material<elem_material_df<true>>, block, 0); break;
     }
     return e == cudaSuccess ? n : 0;
 }

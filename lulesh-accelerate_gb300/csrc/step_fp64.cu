@@ -415,7 +415,10 @@ __global__ void __launch_bounds__(kBlockElem) k_time_constraints(const __grid_co
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long kc = ~0ULL, kh = ~0ULL;
-    if (k < d.ne && !skip_step(d)) constraint_keys(d.ss[k], d.vdov[k], d.arealg[k], d.prm, kc, kh);
+    if (k < d.ne && !skip_step(d)) {
+        if (d.df == kArithDF64) constraint_keys_df(d.ss[k], d.vdov[k], d.arealg[k], d.prm, kc, kh);
+        else constraint_keys(d.ss[k], d.vdov[k], d.arealg[k], d.prm, kc, kh);
+    }
     block_min_publish(kc, kh, d.sc);
 }
 
@@ -485,7 +488,9 @@ void launch_lagrange_nodal(const Dom &d, cudaStream_t st)
 void launch_lagrange_elements(const Dom &d, cudaStream_t st, bool with_constraints)
 {
     launch_elem_kinematics(d, st);
-    if (with_constraints)
+    if (d.df == kArithDF64)
+        launch_elem_material_df(d, st, with_constraints);
+    else if (with_constraints)
         k_elem_material<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     else
         k_elem_material<false><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
@@ -539,7 +544,8 @@ void launch_cycle_timed(const Dom &d, cudaStream_t st, cudaEvent_t ev[7])
     cudaEventRecord(ev[3], st);
     launch_elem_kinematics(d, st);
     cudaEventRecord(ev[4], st);
-    k_elem_material<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    if (d.df == kArithDF64) launch_elem_material_df(d, st, true);
+    else k_elem_material<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     cudaEventRecord(ev[5], st);
     k_finalize<<<1, 1, 0, st>>>(d);
     cudaEventRecord(ev[6], st);
@@ -655,7 +661,7 @@ void launch_rate_probe(int which, float *out, int blocks, int threads, int iters
 void launch_batch_kernel_fp64(const Dom &d, const BatchView &b, cudaStream_t st, int kernel, int cls,
                               LaunchCfg cfg)
 {
-    if (d.df == kArithDF64 && kernel < 3) {
+    if (d.df == kArithDF64) {
         launch_batch_kernel_df(d, b, st, kernel, cls, cfg);
         return;
     }
@@ -670,7 +676,7 @@ void launch_batch_kernel_fp64(const Dom &d, const BatchView &b, cudaStream_t st,
 // Resident blocks per SM of a batched kernel at a block size.
 int batch_max_blocks_fp64(int kernel, int block, int arith)
 {
-    if (arith == kArithDF64 && kernel < 3) return batch_max_blocks_df(kernel, block);
+    if (arith == kArithDF64) return batch_max_blocks_df(kernel, block);
     int n = 0;
     cudaError_t e;
     switch (kernel) {
