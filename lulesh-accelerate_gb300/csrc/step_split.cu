@@ -5,13 +5,16 @@
 //
 //   FP32  shape-function geometry, stress and Flanagan-Belytschko hourglass
 //         corner forces (IntegrateStressForElems, CalcFBHourglassForceForElems,
-//         LULESH-OMP.cc:853-931, :1233-1558), the characteristic length,
-//         the monotonic-Q gradients and limiter (:1799-1862, :2034-2320) and
-//         the sound-speed factor of the viscosity update (:2477-2500);
+//         LULESH-OMP.cc:853-931, :1233-1558), the monotonic-Q gradients and
+//         limiter (:2034-2320);
 //   FP64  node accelerations, velocities and positions (:1613-1683), the
-//         relative volume and its change, the strain rate vdov (:1927-2032),
-//         CalcEnergyForElems / EOS / sound speed / volume update
-//         (:2384-2782) and the constraint minima (:2799-2933).
+//         energy (:2415-2541, accumulated in FP64), the element state and
+//         the constraint minima (:2799-2933); the relative volume and its
+//         change, the strain rate vdov and the characteristic length
+//         (:1799-1862, :1927-2032), the pressure, viscosity and sound speed
+//         of the EOS (:2384-2782) and the constraint candidates are
+//         evaluated to FP64 grade (~2^-47) as double-float pairs on the FP32
+//         pipe (df64.cuh, eos_df.cuh) and stored in FP64.
 //
 // Corner forces are FP32 and summed per node with a compensated (Kahan)
 // FP32 sum whose two words are combined in FP64.  FP32 geometry never sees an
@@ -28,6 +31,7 @@
 #include "kernels.h"
 #include "hexmodes.cuh"
 #include "common.cuh"
+#include "eos_df.cuh"
 #include "batch_kernels.cuh"
 
 #include <cuda_runtime.h>
@@ -121,70 +125,6 @@ __device__ __forceinline__ void df_modes(const float2 *__restrict__ f, const int
         m[4] = df_renorm(df_sum4(df_neg(a), df_neg(b), cc, dd));
         m[5] = df_renorm(df_sum4(df_neg(p), df_neg(q), r, t));
     }
-}
-
-// Mode i of the three coordinates: hi words (FP32), as FP64 (exact), and
-// lo words.
-struct ModeSplit {
-    V3<float> hi, lo;
-    V3<double> hd;
-};
-__device__ __forceinline__ ModeSplit mode_split(const DF mx[6], const DF my[6], const DF mz[6], int i)
-{
-    return {{mx[i].hi, my[i].hi, mz[i].hi}, {mx[i].lo, my[i].lo, mz[i].lo},
-            {f2d(mx[i].hi), f2d(my[i].hi), f2d(mz[i].hi)}};
-}
-
-// 64 x the relative volume change for the lo words, to first order: the
-// volume formula of hexmodes.cuh has the gradient dV64/dM_i = W_i / 3 with
-// W1 = 3 M2xM3 + M4xM5, W2 = 3 M3xM1 + M6xM4, W3 = 3 M1xM2 + M5xM6,
-// W4 = M2xM6 + M5xM1, W5 = M6xM3 + M1xM4, W6 = M4xM2 + M3xM5 (the same
-// vectors as the volume derivative of force_geometry), in FP32 on the hi
-// words, whose shared cross products are C.
-__device__ __forceinline__ float volume64_correction(const ModeSplit M[6], const ModeCrosses<float> &C)
-{
-    const V3<float> &M1 = M[0].hi, &M2 = M[1].hi, &M3 = M[2].hi, &M4 = M[3].hi, &M5 = M[4].hi, &M6 = M[5].hi;
-    auto w3 = [](const V3<float> &c, const V3<float> &e) {
-        return V3<float>{fmaf(3.f, c.x, e.x), fmaf(3.f, c.y, e.y), fmaf(3.f, c.z, e.z)};
-    };
-    const V3<float> W[6] = {w3(C.c23, C.c45), w3(C.c31, C.c64), w3(C.c12, C.c56), cross_sum(M2, M6, M5, M1),
-                            cross_sum(M6, M3, M1, M4), cross_sum(M4, M2, M3, M5)};
-    float s = 0.f;
-#pragma unroll
-    for (int i = 0; i < 6; ++i) s = dot3_acc(M[i].lo, W[i], s);
-    return s * (1.f / 3.f);
-}
-
-// The half-step strain rate (strain_rate of hexmodes.cuh) in FP64 on the hi
-// words of the position and velocity modes, with its numerator and
-// denominator corrected to first order for the lo words in FP32.
-__device__ __forceinline__ double strain_rate_split(const ModeSplit M[3], const ModeSplit V[3], double dt2)
-{
-    const V3<double> A{fma(-dt2, V[0].hd.x, M[0].hd.x), fma(-dt2, V[0].hd.y, M[0].hd.y), fma(-dt2, V[0].hd.z, M[0].hd.z)};
-    const V3<double> B{fma(-dt2, V[1].hd.x, M[1].hd.x), fma(-dt2, V[1].hd.y, M[1].hd.y), fma(-dt2, V[1].hd.z, M[1].hd.z)};
-    const V3<double> C{fma(-dt2, V[2].hd.x, M[2].hd.x), fma(-dt2, V[2].hd.y, M[2].hd.y), fma(-dt2, V[2].hd.z, M[2].hd.z)};
-    const V3<double> cxi = cross3(B, C), cet = cross3(C, A), cze = cross3(A, B);
-    const double num = dot3_acc(cze, V[2].hd, dot3_acc(cet, V[1].hd, dot3(cxi, V[0].hd)));
-    const double den = dot3(B, cet);
-
-    // FP32: the same quantities on the hi words, and the lo words' changes
-    // a, b, c of A, B, C; d(den) = a.(BxC) + b.(CxA) + c.(AxB),
-    // d(num) = d(BxC).V1 + d(CxA).V2 + d(AxB).V3 + (BxC).v1 + (CxA).v2 + (AxB).v3
-    const float h = d2f(dt2);
-    auto half = [h](const V3<float> &m, const V3<float> &v) {
-        return V3<float>{fmaf(-h, v.x, m.x), fmaf(-h, v.y, m.y), fmaf(-h, v.z, m.z)};
-    };
-    const V3<float> Af = half(M[0].hi, V[0].hi), Bf = half(M[1].hi, V[1].hi), Cf = half(M[2].hi, V[2].hi);
-    const V3<float> a = half(M[0].lo, V[0].lo), b = half(M[1].lo, V[1].lo), c = half(M[2].lo, V[2].lo);
-    const V3<float> fxi = cross3(Bf, Cf), fet = cross3(Cf, Af), fze = cross3(Af, Bf);
-    const float dden = dot3_acc(c, fze, dot3_acc(b, fet, dot3(a, fxi)));
-    float dnum = dot3(cross_sum(b, Cf, Bf, c), V[0].hi);
-    dnum = dot3_acc(cross_sum(c, Af, Cf, a), V[1].hi, dnum);
-    dnum = dot3_acc(cross_sum(a, Bf, Af, b), V[2].hi, dnum);
-    dnum = dot3_acc(fxi, V[0].lo, dnum);
-    dnum = dot3_acc(fet, V[1].lo, dnum);
-    dnum = dot3_acc(fze, V[2].lo, dnum);
-    return quot_fast(num + f2d(dnum), den + f2d(dden));
 }
 
 // FP64 state -> hi/lo pairs and reciprocal masses (after any host upload).
@@ -380,68 +320,64 @@ __device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevSc
     int nl[8];
     load_nodelist(d.nodelist, k, nl);
 
-    // FP64: relative volume and the half-step strain rate through the Walsh
-    // modes of the corner coordinates and velocities (CalcKinematicsForElems
-    // :1950-1958, :1975-2020; the identities of hexmodes.cuh).  The modes
-    // come from the hi/lo pairs by compensated FP32 edge sums (df_modes) as
-    // hi + lo with |lo| <= 2^-24 |hi|.  Cross products, volume, strain rate
-    // and the division are FP64 on the hi words (exact in FP64); the lo
-    // words enter through first-order corrections formed in FP32, whose
-    // rounding and neglected second-order terms stay near 2^-47 of the
-    // value, below the ~2^-45 the compensated sums carry.
+    // Relative volume, half-step strain rate and characteristic length
+    // through the Walsh modes of the corner coordinates and velocities
+    // (CalcKinematicsForElems :1950-1958, :1975-2020, CalcElemCharacteristic-
+    // Length :1821-1862; the identities of hexmodes.cuh).  The modes come
+    // from the hi/lo pairs by compensated FP32 edge sums (df_modes) as
+    // hi + lo with |lo| <= 2^-24 |hi|, and the cross products, volume, strain
+    // rate, face areas and divisions run on them as double-float pairs
+    // (df64.cuh): FP64-grade (~2^-47) results without the FP64 pipe.  The
+    // characteristic length sets the Courant time step, which every
+    // instance's result is sensitive to; in FP32 it moved the origin energy of
+    // small ensemble instances (s = 13, 18) up to 1.9e-6 from the reference.
     DF mx[6], my[6], mz[6];
     df_modes<false>(d.xs, nl, mx);
     df_modes<false>(d.ys, nl, my);
     df_modes<false>(d.zs, nl, mz);
-    ModeSplit M[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) M[i] = mode_split(mx, my, mz, i);
     DF vx[6], vy[6], vz[6];
     df_modes<true>(d.xds, nl, vx);
     df_modes<true>(d.yds, nl, vy);
     df_modes<true>(d.zds, nl, vz);
-    ModeSplit V[3];
+    auto pair = [](const DF &a) { return df64(a.hi, a.lo); };
+    V3<df64> M[6], V[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) V[i] = mode_split(vx, vy, vz, i);
-    const ModeCrosses<float> Cf = mode_crosses(M[0].hi, M[1].hi, M[2].hi, M[3].hi, M[4].hi, M[5].hi);
-
-    const double vol64 = volume64_shared(M[0].hd, M[1].hd, M[2].hd,
-                                         mode_crosses(M[0].hd, M[1].hd, M[2].hd, M[3].hd, M[4].hd, M[5].hd));
-    const double volume = (vol64 + f2d(volume64_correction(M, Cf))) * (1.0 / 64.0);
-    // volume / volo, as a product with the reciprocal taken at set-up (within
-    // an ulp of the quotient)
-    const double rel = volume * __ldg(d.inv_volo + k);
+    for (int i = 0; i < 6; ++i) M[i] = {pair(mx[i]), pair(my[i]), pair(mz[i])};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) V[i] = {pair(vx[i]), pair(vy[i]), pair(vz[i])};
+    const ModeCrosses<df64> X = mode_crosses(M[0], M[1], M[2], M[3], M[4], M[5]);
+    const df64 vol64 = volume64_shared(M[0], M[1], M[2], X);
+    // volume / volo, as a product with the reciprocal taken at set-up
+    const df64 rel_df = df_scale(vol64 * to_df(__ldg(d.inv_volo + k)), 1.f / 64.f);
+    const double rel = to_double(rel_df);
     d.vnew[k] = rel;
     d.delv[k] = rel - d.v[k];
-    d.vdov[k] = strain_rate_split(M, V, 0.5 * sc->deltatime);
+    d.vdov[k] = to_double(strain_rate(M[0], M[1], M[2], V[0], V[1], V[2], to_df(0.5 * sc->deltatime)));
+    d.arealg[k] = to_double(df_scale(vol64, 0.25f) * df_rsqrt(max_face_cross2_64(M[0], M[1], M[2], M[3], M[4], M[5], X)));
     if (rel <= 0.0) flag_error(sc, ERR_K3_VNEW, k);
 
-    // FP32: characteristic length and monotonic-Q gradients (:1821-1862,
-    // :2034-2180) through the hi words of the modes, with the formulas of the
-    // FP64 kernel (face areas from the shared cross products; the logical
-    // differences are M/4, so each cross product is (M x M')/16 and each
-    // velocity difference Mv/4).  The roots are the correctly rounded sqrtf
-    // and division: with the approximate rsqrtf (2 ulps) the characteristic
-    // length and the Q lengths moved the origin energies of small ensemble
-    // instances (s = 13..26) up to 2.2e-6 from FP64, against <= 1e-7 here.
-    const float vol = d2f(volume);
-    d.arealg[k] = f2d((16.f * vol) / sqrtf(max_face_cross2_64(M[0].hi, M[1].hi, M[2].hi, M[3].hi, M[4].hi, M[5].hi, Cf)));
+    // FP32: monotonic-Q gradients (:2034-2180) through the high words of the
+    // modes' cross products, with the formulas of the FP64 kernel (the
+    // logical differences are M/4, so each cross product is (M x M')/16 and
+    // each velocity difference Mv/4); the roots are the correctly rounded
+    // sqrtf and division.
+    auto hi3 = [](const V3<df64> &v) { return V3<float>{v.x.hi, v.y.hi, v.z.hi}; };
+    const V3<float> c12 = hi3(X.c12), c23 = hi3(X.c23), c31 = hi3(X.c31);
+    const V3<float> V1 = hi3(V[0]), V2 = hi3(V[1]), V3f = hi3(V[2]);
+    const float vol = vol64.hi * (1.f / 64.f);
     const float ptiny = 1.e-36f;
     const float vscale = 1.f / fmaf(vol, 64.f, 64.f * ptiny);     // (1/16) (1/4) / (vol + ptiny)
     float *gq = d.gq;
-    gq[5 * ne + k] = vol / sqrtf(fmaf(0.00390625f, dot3(Cf.c12, Cf.c12), ptiny));   // delx_zeta
-    gq[2 * ne + k] = vscale * dot3(Cf.c12, V[2].hi);                                 // delv_zeta
-    gq[3 * ne + k] = vol / sqrtf(fmaf(0.00390625f, dot3(Cf.c23, Cf.c23), ptiny));   // delx_xi
-    gq[0 * ne + k] = vscale * dot3(Cf.c23, V[0].hi);                                 // delv_xi
-    gq[4 * ne + k] = vol / sqrtf(fmaf(0.00390625f, dot3(Cf.c31, Cf.c31), ptiny));   // delx_eta
-    gq[1 * ne + k] = vscale * dot3(Cf.c31, V[1].hi);                                 // delv_eta
+    gq[5 * ne + k] = vol / sqrtf(fmaf(0.00390625f, dot3(c12, c12), ptiny));   // delx_zeta
+    gq[2 * ne + k] = vscale * dot3(c12, V3f);                                 // delv_zeta
+    gq[3 * ne + k] = vol / sqrtf(fmaf(0.00390625f, dot3(c23, c23), ptiny));   // delx_xi
+    gq[0 * ne + k] = vscale * dot3(c23, V1);                                  // delv_xi
+    gq[4 * ne + k] = vol / sqrtf(fmaf(0.00390625f, dot3(c31, c31), ptiny));   // delx_eta
+    gq[1 * ne + k] = vscale * dot3(c31, V2);                                  // delv_eta
 }
 
-// Held to 80 registers (six blocks per SM; a few hundred bytes spilled):
-// with its FP64 work cut by the first-order corrections the kernel waits on
-// its corner gathers, and the extra resident blocks pay (1.27 -> 1.15 ms at
-// s=192 against the unbounded 128 registers; eight blocks spill too much).
-__global__ void __launch_bounds__(kBlockElem, 6) k_elem_kinematics_split(const __grid_constant__ Dom d)
+// Four blocks per SM (128 registers, no spills: the pairs need them).
+__global__ void __launch_bounds__(kBlockElem, 4) k_elem_kinematics_split(const __grid_constant__ Dom d)
 {
     if (skip_step(d)) return;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -450,7 +386,7 @@ __global__ void __launch_bounds__(kBlockElem, 6) k_elem_kinematics_split(const _
 }
 
 // ---------------------------------------------------------------------
-// Q limiter in FP32, EOS and constraints in FP64
+// Q limiter in FP32; EOS and constraints in pairs, the energy in FP64
 // ---------------------------------------------------------------------
 template <bool kConstraints>
 __device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScalars *sc,
@@ -473,7 +409,7 @@ __device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScal
                                                  BC_ZETA_P_FREE, __ldg(d.lzetam + k), __ldg(d.lzetap + k),
                                                  lim, maxs);
         const double vnew = d.vnew[k], vdov = d.vdov[k];
-        double qlin = 0., qquad = 0.;
+        float qlin = 0.f, qquad = 0.f;
         if (!gt(vdov, 0.)) {
             float dxi = dv_xi[k] * d.gq[3 * ne + k];
             float deta = dv_eta[k] * d.gq[4 * ne + k];
@@ -485,24 +421,25 @@ __device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScal
             const float sl = (dxi * (1.f - phixi) + deta * (1.f - phieta)) + dzeta * (1.f - phizeta);
             const float sq = (dxi * dxi * (1.f - phixi * phixi) + deta * deta * (1.f - phieta * phieta)) +
                              dzeta * dzeta * (1.f - phizeta * phizeta);
-            qlin = f2d(-d2f(P.qlc_monoq) * rho * sl);
-            qquad = f2d(d2f(P.qqc_monoq) * rho * sq);
+            qlin = -d2f(P.qlc_monoq) * rho * sl;
+            qquad = d2f(P.qqc_monoq) * rho * sq;
         }
         if (d.keep & 2) {
-            d.ql[k] = qlin;
-            d.qq[k] = qquad;
+            d.ql[k] = f2d(qlin);
+            d.qq[k] = f2d(qquad);
         }
-        const double ssn = material_update<true>(d, k, sc, vnew, qlin, qquad, d.reps ? __ldg(d.reps + k) : 1);
-        if (kConstraints) constraint_keys(ssn, vdov, d.arealg[k], P, kc, kh);
+        // the EOS, energy, sound speed and constraint candidates in pairs,
+        // the energy accumulated in FP64 (eos_df.cuh)
+        const double ssn = material_update_df(d, k, sc, vnew, df64(qlin, 0.f), df64(qquad, 0.f),
+                                              d.reps ? __ldg(d.reps + k) : 1);
+        if (kConstraints) constraint_keys_df(ssn, vdov, d.arealg[k], P, kc, kh);
     }
 }
 
-// The split material kernel waits on its neighbour gathers (the limiter) and
-// its FP64 chain more than it fills the FP64 pipe, so it is held to 64
-// registers: eight 128-thread blocks per SM instead of six, 0.89 -> 0.78 ms
-// at s=192.
+// Six blocks per SM (85 registers: the EOS in pairs needs more than the 64
+// the FP64 one was held to).
 template <bool kConstraints>
-__global__ void __launch_bounds__(kBlockElem, 8) k_elem_material_split(const __grid_constant__ Dom d)
+__global__ void __launch_bounds__(kBlockElem, 6) k_elem_material_split(const __grid_constant__ Dom d)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long kc = ~0ULL, kh = ~0ULL;
@@ -573,7 +510,7 @@ void launch_batch_kernel_split(const Dom &d, const BatchView &b, cudaStream_t st
     case 0: kb_elem<elem_force_split><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     case 1: kb_node<node_update_split><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     case 2: kb_elem_capped<elem_kinematics_split, 2><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
-    default: kb_material_capped<elem_material_split<true>, 4><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    default: kb_material_capped<elem_material_split<true>, 3><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     }
 }
 
@@ -586,7 +523,7 @@ int batch_max_blocks_split(int kernel, int block)
     case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_force_split>, block, 0); break;
     case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_node<node_update_split>, block, 0); break;
     case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem_capped<elem_kinematics_split, 2>, block, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material_capped<elem_material_split<true>, 4>, block, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material_capped<elem_material_split<true>, 3>, block, 0); break;
     }
     return e == cudaSuccess ? n : 0;
 }
