@@ -144,21 +144,72 @@ __global__ void __launch_bounds__(kBlockNode) k_split_sync(const __grid_constant
 // ---------------------------------------------------------------------
 // Element force in FP32
 // ---------------------------------------------------------------------
-__device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars *sc)
+// The hi/lo pairs of field f: 0..5 = x, y, z, xd, yd, zd.
+__device__ __forceinline__ const float2 *pair_field(const Dom &d, int f)
+{
+    return f == 0 ? d.xs : f == 1 ? d.ys : f == 2 ? d.zs : f == 3 ? d.xds : f == 4 ? d.yds : d.zds;
+}
+
+// An element's corner values relative to corner 0, gathered from global
+// memory through its node list (any mesh).
+struct GlobalCorners {
+    const Dom &d;
+    int nl[8];
+    __device__ GlobalCorners(const Dom &dom, int k) : d(dom) { load_nodelist(d.nodelist, k, nl); }
+    __device__ void rel(int f, float out[8]) const { rel8(pair_field(d, f), nl, out); }
+};
+
+// Staged tile of a structured cube: the force kernel's block covers
+// kTileRows x kTileCols elements of one plane, whose corners are the
+// 2 x (kTileRows+1) x (kTileCols+1) nodes of the tile, loaded once into
+// shared memory (coalesced along the rows) instead of gathered eight times
+// per element.
+constexpr int kTileCols = 64, kTileRows = 2;
+constexpr int kTileNodeCols = kTileCols + 1, kTileNodeRows = kTileRows + 1;
+constexpr int kTileNodes = 2 * kTileNodeRows * kTileNodeCols;
+
+struct TileCorners {
+    const float2 *tile;   // [6][kTileNodes]
+    int li[8];            // the corners' places in the tile, in the reference's corner order
+    __device__ TileCorners(const float2 *t, int rr, int cc) : tile(t)
+    {
+        const int b = rr * kTileNodeCols + cc, up = kTileNodeRows * kTileNodeCols;
+        li[0] = b;
+        li[1] = b + 1;
+        li[2] = b + kTileNodeCols + 1;
+        li[3] = b + kTileNodeCols;
+        li[4] = b + up;
+        li[5] = b + up + 1;
+        li[6] = b + up + kTileNodeCols + 1;
+        li[7] = b + up + kTileNodeCols;
+    }
+    __device__ void rel(int f, float out[8]) const
+    {
+        const float2 *t = tile + f * kTileNodes;
+        const float2 a0 = t[li[0]];
+        out[0] = 0.f;
+#pragma unroll
+        for (int c = 1; c < 8; ++c) {
+            const float2 a = t[li[c]];
+            out[c] = (a.x - a0.x) + (a.y - a0.y);
+        }
+    }
+};
+
+template <class Corners>
+__device__ __forceinline__ void elem_force_split_from(const Dom &d, int k, DevScalars *sc, const Corners &cn)
 {
     const size_t ne = (size_t)d.ne;
 
-    int nl[8];
-    load_nodelist(d.nodelist, k, nl);
     // The geometry of the FP64 kernel (the Walsh-mode identities of
     // hexmodes.cuh) in FP32, on corner coordinates relative to corner 0: the
     // modes M1..M7 do not see a translation.
     V3<float> M[7];
     {
         float x[8], y[8], z[8], mx[7], my[7], mz[7];
-        rel8(d.xs, nl, x);
-        rel8(d.ys, nl, y);
-        rel8(d.zs, nl, z);
+        cn.rel(0, x);
+        cn.rel(1, y);
+        cn.rel(2, z);
         walsh8(x, mx);
         walsh8(y, my);
         walsh8(z, mz);
@@ -219,11 +270,10 @@ __device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars
         const float coefficient = (((-hourg) * 0.01f) * d2f(d.ss[k])) * d2f(d.elem_mass[k]) * r;
         // velocities relative to corner 0: the hourglass modes are blind to
         // a uniform velocity (sum over corners of each hourgam column is 0)
-        const float2 *vel[3] = {d.xds, d.yds, d.zds};
 #pragma unroll
         for (int dim = 0; dim < 3; ++dim) {
             float u[8];
-            rel8(vel[dim], nl, u);
+            cn.rel(3 + dim, u);
             float h[4];
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
@@ -243,6 +293,43 @@ __device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars
         d.f32y[c * ne + k] = f[1][c];
         d.f32z[c * ne + k] = f[2][c];
     }
+}
+
+__device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars *sc)
+{
+    elem_force_split_from(d, k, sc, GlobalCorners(d, k));
+}
+
+// The staged force kernel of a structured s^3 cube (Dom::s > 0, the node
+// and element numbering of the reference's set-up): block b covers plane p,
+// rows r0..r0+1 and columns c0..c0+63 of elements.  The same arithmetic as
+// k_elem_force_split, so the same bits.  The skip decision is taken once
+// per block (an error word another block sets meanwhile must not split the
+// block at its barrier).
+__global__ void __launch_bounds__(kBlockElem, 8) k_elem_force_split_tiled(const __grid_constant__ Dom d)
+{
+    __shared__ float2 tile[6 * kTileNodes];
+    __shared__ int skip;
+    const int s = d.s, en = s + 1;
+    const int nbc = (s + kTileCols - 1) / kTileCols, nbr = (s + kTileRows - 1) / kTileRows;
+    const int cb = blockIdx.x % nbc, rb = (blockIdx.x / nbc) % nbr, p = blockIdx.x / (nbc * nbr);
+    const int r0 = rb * kTileRows, c0 = cb * kTileCols;
+    if (threadIdx.x == 0) skip = skip_step(d) ? 1 : 0;
+    for (int i = threadIdx.x; i < kTileNodes; i += blockDim.x) {
+        const int dc = i % kTileNodeCols, dr = (i / kTileNodeCols) % kTileNodeRows, dp = i / (kTileNodeCols * kTileNodeRows);
+        const int r = r0 + dr, c = c0 + dc;
+        if (r <= s && c <= s) {
+            const long n = ((long)(p + dp) * en + r) * en + c;
+#pragma unroll
+            for (int f = 0; f < 6; ++f) tile[f * kTileNodes + i] = __ldg(pair_field(d, f) + n);
+        }
+    }
+    __syncthreads();
+    const int rr = threadIdx.x / kTileCols, cc = threadIdx.x % kTileCols;
+    const int r = r0 + rr, c = c0 + cc;
+    if (skip || rr >= kTileRows || r >= s || c >= s) return;
+    const int k = (p * s + r) * s + c;
+    elem_force_split_from(d, k, d.sc, TileCorners(tile, rr, cc));
 }
 
 // The FP32 force kernel waits on its corner gathers rather than on an
@@ -455,6 +542,19 @@ __global__ void __launch_bounds__(kBlockElem, 6) k_elem_material_split(const __g
 // ---------------------------------------------------------------------
 static inline unsigned blocks_for(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// The force kernel: staged tiles on structured cubes wide enough to fill
+// them (s >= 64 columns), the gather kernel otherwise (unstructured meshes,
+// small cubes).
+static void launch_elem_force_split(const Dom &d, cudaStream_t st)
+{
+    if (d.s >= kTileCols) {
+        const long nb = (long)d.s * ((d.s + kTileRows - 1) / kTileRows) * ((d.s + kTileCols - 1) / kTileCols);
+        k_elem_force_split_tiled<<<(unsigned)nb, kTileRows * kTileCols, 0, st>>>(d);
+    } else {
+        k_elem_force_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    }
+}
+
 void launch_split_sync(const Dom &d, cudaStream_t st)
 {
     k_split_sync<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
@@ -462,7 +562,7 @@ void launch_split_sync(const Dom &d, cudaStream_t st)
 
 void launch_lagrange_nodal_split(const Dom &d, cudaStream_t st)
 {
-    k_elem_force_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    launch_elem_force_split(d, st);
     k_node_update_split<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
 }
 
@@ -488,7 +588,7 @@ void launch_cycle_timed_split(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTim
     cudaEventRecord(ev[0], st);
     launch_time_increment(d, st);
     cudaEventRecord(ev[1], st);
-    k_elem_force_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    launch_elem_force_split(d, st);
     cudaEventRecord(ev[2], st);
     k_node_update_split<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
     cudaEventRecord(ev[3], st);
