@@ -320,6 +320,26 @@ def batch_legs(pkg, torch, args, barrier, max_over_ranks, ref_runs: dict) -> dic
         tuning = b.tuning()
         b.close()
 
+        # the same ensemble, its launch shapes re-timed whenever the running
+        # instances' elements fall below half of those last tuned for (the
+        # re-tuning inside the timed region)
+        retuned = None
+        if not args.no_retune:
+            with pkg.Batch(sizes, scale, pkg.INIT_V2, prec) as rb:
+                rb.autotune(str(cache))
+                rst = torch.cuda.ExternalStream(rb.stream)
+                r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                barrier()
+                r0.record(rst)
+                _, n_retunes = rb.run_retuned(chunk=args.retune_chunk, fraction=0.5)
+                r1.record(rst)
+                barrier()
+                rms = max_over_ranks(r0.elapsed_time(r1))
+                retuned = {"value": rb.zone_cycles() / (rms * 1e-3) * 1e-6, "unit": UNIT, "ms": rms,
+                           "retunes": n_retunes, "chunk_cycles": args.retune_chunk,
+                           "rule": "re-time the launch shapes when the running elements fall below half of "
+                                   "those last tuned for"}
+
         # one at a time on the plain FP64 path, sampled per size band
         def solo(i):
             g = pkg.Lulesh(int(sizes[i]), pkg.INIT_V2, pkg.FP64)
@@ -367,7 +387,7 @@ def batch_legs(pkg, torch, args, barrier, max_over_ranks, ref_runs: dict) -> dic
                                       "weighting": "each size band's sampled rate weighted by the band's share "
                                                    "of the ensemble's zone-cycles"},
                "speedup_vs_one_at_a_time_fp64": value / solo_rate, "gpu_launches": launches,
-               "autotuned": tuning}
+               "autotuned": tuning, "retuned": retuned}
 
         # every instance the reference ran, against its own answer
         refs = ref_runs.get(name, [])
@@ -452,6 +472,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the 500-cycle runs compared with the reference's own")
     ap.add_argument("--no-ieee", action="store_true", help="skip the all-IEEE-FP64 leg")
+    ap.add_argument("--no-retune", action="store_true", help="skip the re-tuned ensemble runs")
+    ap.add_argument("--retune-chunk", type=int, default=200, help="cycles between re-tuning checks")
     ap.add_argument("--cpu-cycles", type=int, default=40,
                     help="cycles of the CPU baseline sample (about 10 s of the 16-core host at s=192)")
     ap.add_argument("--no-cpu", action="store_true")
@@ -737,6 +759,8 @@ def summary_of(line: dict) -> dict:
     for name, leg in (line.get("batched") or {}).items():
         out[name] = {"value": round(leg["value"], 1),
                      "speedup_vs_one_at_a_time_fp64": round(leg["speedup_vs_one_at_a_time_fp64"], 3)}
+        if leg.get("retuned"):
+            out[name]["retuned"] = round(leg["retuned"]["value"], 1)
         if leg.get("origin_energy_error_vs_reference"):
             e = leg["origin_energy_error_vs_reference"]
             out[name]["origin_energy_error_max"] = e["max"]

@@ -223,7 +223,9 @@ int lulesh_get_regions(lulesh_ctx *ctx, int *reg_num_list);
 int lulesh_region_numbers(long num_elem, int num_regions, int balance, int *reg_num_list);
 
 /* ---- the step API ---------------------------------------------------- */
-int lulesh_time_increment(lulesh_ctx *ctx);        /* TimeIncrement      LULESH-OMP.cc:557-604   */
+int lulesh_time_increment(lulesh_ctx *ctx);        /* TimeIncrement      LULESH-OMP.cc:557-604;
+                                                      returns without waiting for the GPU (it has
+                                                      no error exit of its own)                */
 int lulesh_lagrange_nodal(lulesh_ctx *ctx);        /* LagrangeNodal      LULESH-OMP.cc:1685-1704 */
 int lulesh_lagrange_elements(lulesh_ctx *ctx);     /* LagrangeElements   LULESH-OMP.cc:2784-2797 */
 int lulesh_calc_time_constraints(lulesh_ctx *ctx); /* CalcTimeConstraintsForElems :2935-2942   */
@@ -378,7 +380,8 @@ int lulesh_batch_run(lulesh_batch *b, int max_cycles, int *cycles_done);
 int lulesh_batch_size(lulesh_batch *b, int *n, long *total_elements, long *total_nodes);
 int lulesh_batch_instance(lulesh_batch *b, int i, lulesh_scalars *out, double *origin_energy, int *status);
 int lulesh_batch_get_field(lulesh_batch *b, int i, const char *name, double *host, long n);
-/* Sum over instances of elements x cycles done. */
+/* Sum over instances of elements x cycles done by the last lulesh_batch_run
+ * or lulesh_batch_run_retuned call. */
 int lulesh_batch_zone_cycles(lulesh_batch *b, double *zone_cycles);
 
 /* Choose threads per block (64/128/256, i.e. 4/2/1 elements per thread of a
@@ -388,6 +391,16 @@ int lulesh_batch_zone_cycles(lulesh_batch *b, double *zone_cycles);
  * (keyed by GPU model, SM count, precision, class, kernel; NULL: no cache);
  * retune != 0 ignores cached entries. */
 int lulesh_batch_autotune(lulesh_batch *b, const char *cache_path, int retune);
+
+/* lulesh_batch_run in chunks of at most chunk cycles; after a chunk, when the
+ * elements of the instances still running have fallen below fraction
+ * (0 < fraction < 1) of those the launch shapes were last tuned for, the
+ * shapes are re-timed on the running set (lulesh_batch_autotune, not
+ * cached) and the graph rebuilt.  Results are those of lulesh_batch_run:
+ * the launch shapes change no element's arithmetic.  *cycles_done: the
+ * largest per-instance count; *retunes: how many re-tunings ran. */
+int lulesh_batch_run_retuned(lulesh_batch *b, int chunk, double fraction, int max_cycles, int *cycles_done,
+                             int *retunes);
 int lulesh_batch_tuning(lulesh_batch *b, int size_class, int kernel, int *block, int *grid);
 
 void *lulesh_batch_stream(lulesh_batch *b);

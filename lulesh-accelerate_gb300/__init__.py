@@ -164,6 +164,8 @@ _SIGNATURES = {
     "lulesh_batch_get_field": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, _dp, C.c_long]),
     "lulesh_batch_zone_cycles": (C.c_int, [C.c_void_p, _dp]),
     "lulesh_batch_autotune": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
+    "lulesh_batch_run_retuned": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int)]),
     "lulesh_batch_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "lulesh_batch_stream": (C.c_void_p, [C.c_void_p]),
     "lulesh_batch_kernel_launches": (C.c_longlong, [C.c_void_p]),
@@ -578,6 +580,15 @@ class Batch:
         zc = C.c_double()
         _check_batch(load_library().lulesh_batch_zone_cycles(self._h, C.byref(zc)), self._h)
         return zc.value
+
+    def run_retuned(self, chunk: int = 200, fraction: float = 0.5, max_cycles: int = 0) -> tuple[int, int]:
+        """Run in chunks of cycles, re-tuning the launch shapes whenever the
+        running instances' elements fall below ``fraction`` of those last
+        tuned for; returns (largest per-instance cycle count, re-tunings)."""
+        n, r = C.c_int(), C.c_int()
+        _check_batch(load_library().lulesh_batch_run_retuned(self._h, chunk, fraction, max_cycles, C.byref(n),
+                                                             C.byref(r)), self._h)
+        return n.value, r.value
 
     def autotune(self, cache_path: str | None = None, retune: bool = False):
         path = None if cache_path is None else str(cache_path).encode()

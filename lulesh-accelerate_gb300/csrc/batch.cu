@@ -65,6 +65,7 @@ struct lulesh_batch {
     long long launches = 0;
     int kernels_per_cycle = 0;
     bool tuned = false;
+    double last_zc = 0.0;   // elements x cycles of the last run call
     std::string err;
 };
 
@@ -677,9 +678,11 @@ int lulesh_batch_run(lulesh_batch *b, int max_cycles, int *cycles_done)
     BCK(cudaStreamSynchronize(b->stream));
     int most = 0;
     long long total = 0;
+    b->last_zc = 0.0;
     for (int i = 0; i < b->n; ++i) {
         most = std::max(most, b->h_sc[i].run_cycles);
         total += b->h_sc[i].run_cycles;
+        b->last_zc += (double)b->ne_i[i] * b->h_sc[i].run_cycles;
     }
     if (cycles_done) *cycles_done = most;
     // time increment, epilogue and compaction run every cycle; each step
@@ -697,6 +700,55 @@ int lulesh_batch_run(lulesh_batch *b, int max_cycles, int *cycles_done)
                      "lulesh_batch_run: instance " + std::to_string(i) + " stopped short of stoptime (" +
                          (h.deltatime > 0.0 ? "cycle budget ran out" : "time step no longer positive") + ")");
     }
+    return LULESH_OK;
+}
+
+int lulesh_batch_run_retuned(lulesh_batch *b, int chunk, double fraction, int max_cycles, int *cycles_done,
+                             int *retunes)
+{
+    if (!b || chunk < 1 || !(fraction > 0.0 && fraction < 1.0)) return LULESH_ERR_ARG;
+    if (cycles_done) *cycles_done = 0;
+    if (retunes) *retunes = 0;
+    // elements of the instances still running (the host copy of the scalars
+    // is current after every run call)
+    auto running = [&]() {
+        long m = 0;
+        for (int i = 0; i < b->n; ++i) {
+            const DevScalars &h = b->h_sc[i];
+            if (!h.err_any && h.time < b->dom.prm.stoptime && h.deltatime > 0.0) m += b->ne_i[i];
+        }
+        return m;
+    };
+    BCK(cudaMemcpyAsync(b->h_sc, b->dom.sc, sizeof(DevScalars) * b->n, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    long tuned_for = running();
+    std::vector<long long> done_i(b->n, 0);
+    long long total = 0;
+    int n_retunes = 0;
+    double zc = 0.0;
+    for (;;) {
+        int cap = chunk;
+        if (max_cycles > 0) cap = (int)std::min<long long>(chunk, max_cycles - total);
+        int most = 0;
+        int rc = lulesh_batch_run(b, cap, &most);
+        for (int i = 0; i < b->n; ++i) done_i[i] += b->h_sc[i].run_cycles;
+        total += most;
+        zc += b->last_zc;
+        b->last_zc = zc;
+        if (rc) return rc;
+        const long now = running();
+        if (now == 0 || most == 0 || (max_cycles > 0 && total >= max_cycles)) break;
+        if (now < fraction * tuned_for) {
+            // the running set shrank: re-time the launch shapes on it (not
+            // cached: they belong to this part of this run) and rebuild the
+            // graph
+            if ((rc = lulesh_batch_autotune(b, nullptr, 1))) return rc;
+            tuned_for = now;
+            ++n_retunes;
+        }
+    }
+    if (cycles_done) *cycles_done = (int)*std::max_element(done_i.begin(), done_i.end());
+    if (retunes) *retunes = n_retunes;
     return LULESH_OK;
 }
 
@@ -762,11 +814,7 @@ int lulesh_batch_get_field(lulesh_batch *b, int i, const char *name, double *hos
 int lulesh_batch_zone_cycles(lulesh_batch *b, double *zone_cycles)
 {
     if (!b || !zone_cycles) return LULESH_ERR_ARG;
-    BCK(cudaMemcpyAsync(b->h_sc, b->dom.sc, sizeof(DevScalars) * b->n, cudaMemcpyDeviceToHost, b->stream));
-    BCK(cudaStreamSynchronize(b->stream));
-    double zc = 0.0;
-    for (int i = 0; i < b->n; ++i) zc += (double)b->ne_i[i] * b->h_sc[i].run_cycles;
-    *zone_cycles = zc;
+    *zone_cycles = b->last_zc;
     return LULESH_OK;
 }
 

@@ -103,3 +103,21 @@ def test_batch_of_tiny_and_single_instances(pkg):
                 for k in ("x", "e", "p", "v"):
                     assert np.array_equal(b.get_field(i, k), g.get_field(k)), (sizes, i, k)
                 g.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_retuned_run_equals_plain_run(pkg, precision):
+    """Re-tuning the launch shapes as instances retire changes no element's
+    arithmetic: the chunked, re-tuned run ends in the same bits and cycle
+    counts as one run."""
+    prec = pkg.FP64 if precision == "fp64" else pkg.SPLIT
+    with pkg.Batch(SIZES, SCALE, pkg.INIT_V2, prec) as a, pkg.Batch(SIZES, SCALE, pkg.INIT_V2, prec) as b:
+        most = a.run()
+        most_b, retunes = b.run_retuned(chunk=60, fraction=0.95)
+        assert most_b == most
+        assert retunes >= 1
+        assert b.zone_cycles() == a.zone_cycles()
+        for i in range(len(SIZES)):
+            assert a.instance(i)[0].cycle == b.instance(i)[0].cycle
+            for k in ("x", "xd", "e", "p", "q", "v", "ss"):
+                assert np.array_equal(a.get_field(i, k), b.get_field(i, k)), (i, k)
