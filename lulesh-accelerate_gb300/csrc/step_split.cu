@@ -32,6 +32,7 @@
 #include "hexmodes.cuh"
 #include "common.cuh"
 #include "eos_df.cuh"
+#include "tile.cuh"
 #include "batch_kernels.cuh"
 
 #include <cuda_runtime.h>
@@ -159,30 +160,10 @@ struct GlobalCorners {
     __device__ void rel(int f, float out[8]) const { rel8(pair_field(d, f), nl, out); }
 };
 
-// Staged tile of a structured cube: the force kernel's block covers
-// kTileRows x kTileCols elements of one plane, whose corners are the
-// 2 x (kTileRows+1) x (kTileCols+1) nodes of the tile, loaded once into
-// shared memory (coalesced along the rows) instead of gathered eight times
-// per element.
-constexpr int kTileCols = 64, kTileRows = 2;
-constexpr int kTileNodeCols = kTileCols + 1, kTileNodeRows = kTileRows + 1;
-constexpr int kTileNodes = 2 * kTileNodeRows * kTileNodeCols;
-
 struct TileCorners {
     const float2 *tile;   // [6][kTileNodes]
     int li[8];            // the corners' places in the tile, in the reference's corner order
-    __device__ TileCorners(const float2 *t, int rr, int cc) : tile(t)
-    {
-        const int b = rr * kTileNodeCols + cc, up = kTileNodeRows * kTileNodeCols;
-        li[0] = b;
-        li[1] = b + 1;
-        li[2] = b + kTileNodeCols + 1;
-        li[3] = b + kTileNodeCols;
-        li[4] = b + up;
-        li[5] = b + up + 1;
-        li[6] = b + up + kTileNodeCols + 1;
-        li[7] = b + up + kTileNodeCols;
-    }
+    __device__ TileCorners(const float2 *t, int rr, int cc) : tile(t) { tile_corners(rr, cc, li); }
     __device__ void rel(int f, float out[8]) const
     {
         const float2 *t = tile + f * kTileNodes;
@@ -306,29 +287,16 @@ __device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars
 // k_elem_force_split, so the same bits.  The skip decision is taken once
 // per block (an error word another block sets meanwhile must not split the
 // block at its barrier).
-__global__ void __launch_bounds__(kBlockElem, 8) k_elem_force_split_tiled(const __grid_constant__ Dom d)
+__global__ void __launch_bounds__(kTileThreads, 8) k_elem_force_split_tiled(const __grid_constant__ Dom d)
 {
     __shared__ float2 tile[6 * kTileNodes];
     __shared__ int skip;
-    const int s = d.s, en = s + 1;
-    const int nbc = (s + kTileCols - 1) / kTileCols, nbr = (s + kTileRows - 1) / kTileRows;
-    const int cb = blockIdx.x % nbc, rb = (blockIdx.x / nbc) % nbr, p = blockIdx.x / (nbc * nbr);
-    const int r0 = rb * kTileRows, c0 = cb * kTileCols;
+    const TileCoord t = tile_coord(d.s);
     if (threadIdx.x == 0) skip = skip_step(d) ? 1 : 0;
-    for (int i = threadIdx.x; i < kTileNodes; i += blockDim.x) {
-        const int dc = i % kTileNodeCols, dr = (i / kTileNodeCols) % kTileNodeRows, dp = i / (kTileNodeCols * kTileNodeRows);
-        const int r = r0 + dr, c = c0 + dc;
-        if (r <= s && c <= s) {
-            const long n = ((long)(p + dp) * en + r) * en + c;
-#pragma unroll
-            for (int f = 0; f < 6; ++f) tile[f * kTileNodes + i] = __ldg(pair_field(d, f) + n);
-        }
-    }
+    load_tile(tile, d.s, t, 0, 6, [&](int f) { return pair_field(d, f); });
     __syncthreads();
-    const int rr = threadIdx.x / kTileCols, cc = threadIdx.x % kTileCols;
-    const int r = r0 + rr, c = c0 + cc;
-    if (skip || rr >= kTileRows || r >= s || c >= s) return;
-    const int k = (p * s + r) * s + c;
+    int k, rr, cc;
+    if (skip || !tile_element(d.s, t, k, rr, cc)) return;
     elem_force_split_from(d, k, d.sc, TileCorners(tile, rr, cc));
 }
 
@@ -548,8 +516,7 @@ static inline unsigned blocks_for(long n, int bs) { return (unsigned)((n + bs - 
 static void launch_elem_force_split(const Dom &d, cudaStream_t st)
 {
     if (d.s >= kTileCols) {
-        const long nb = (long)d.s * ((d.s + kTileRows - 1) / kTileRows) * ((d.s + kTileCols - 1) / kTileCols);
-        k_elem_force_split_tiled<<<(unsigned)nb, kTileRows * kTileCols, 0, st>>>(d);
+        k_elem_force_split_tiled<<<(unsigned)tile_blocks(d.s), kTileThreads, 0, st>>>(d);
     } else {
         k_elem_force_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     }

@@ -121,3 +121,4 @@ def test_retuned_run_equals_plain_run(pkg, precision):
             assert a.instance(i)[0].cycle == b.instance(i)[0].cycle
             for k in ("x", "xd", "e", "p", "q", "v", "ss"):
                 assert np.array_equal(a.get_field(i, k), b.get_field(i, k)), (i, k)
+
