@@ -84,6 +84,25 @@ __device__ __forceinline__ df64 df_fma(df64 a, df64 b, df64 c)
     return fast_two_sum(s.hi, __fadd_rn(__fadd_rn(s.lo, t), c.lo));
 }
 
+// A sum of products c + sum_i a_i b_i accumulated with one renormalisation
+// at the end: each product's high word joins the running high word through
+// two_sum and every low-order term collects in one float (the compensated
+// dot product Dot2 of Ogita, Rump and Oishi, 2005, on pairs).  12 FP32
+// operations per term against 15 for a chain of df_fma, to the same order
+// of accuracy.
+struct DfDot {
+    float s, e;
+    __device__ explicit DfDot(df64 c) : s(c.hi), e(c.lo) {}
+    __device__ void add(df64 a, df64 b)
+    {
+        const df64 p = two_prod(a.hi, b.hi);
+        const df64 q = two_sum(s, p.hi);
+        s = q.hi;
+        e = __fadd_rn(e, __fadd_rn(q.lo, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo))));
+    }
+    __device__ df64 value() const { return two_sum(s, e); }
+};
+
 // a times a float (exact in hi)
 __device__ __forceinline__ df64 df_mul_f(df64 a, float b)
 {

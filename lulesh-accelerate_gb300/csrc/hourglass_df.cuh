@@ -41,8 +41,13 @@ __device__ __forceinline__ void fb_hourglass_df(const Dom &d, const int nl[8], c
         // three multiply-adds
         const df64 hx = -(volinv192 * H[m].x), hy = -(volinv192 * H[m].y), hz = -(volinv192 * H[m].z);
 #pragma unroll
-        for (int c = 0; c < 8; ++c)
-            hg[c][m] = fma(dvdz[c], hz, fma(dvdy[c], hy, fma(dvdx[c], hx, df64(gam[m][c], 0.f))));
+        for (int c = 0; c < 8; ++c) {
+            DfDot acc(df64(gam[m][c], 0.f));
+            acc.add(dvdx[c], hx);
+            acc.add(dvdy[c], hy);
+            acc.add(dvdz[c], hz);
+            hg[c][m] = acc.value();
+        }
     }
     // One velocity component per iteration, the loop kept rolled: the body is
     // the same code three times over, and the smaller instruction footprint
@@ -60,15 +65,19 @@ __device__ __forceinline__ void fb_hourglass_df(const Dom &d, const int nl[8], c
         df64 h[4];
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            df64 acc = hg[0][m] * u[0];
+            DfDot acc(df64(0.f, 0.f));
 #pragma unroll
-            for (int c = 1; c < 8; ++c) acc = fma(hg[c][m], u[c], acc);
-            h[m] = coefficient * acc;
+            for (int c = 0; c < 8; ++c) acc.add(hg[c][m], u[c]);
+            h[m] = coefficient * acc.value();
         }
         df64 f[8];
 #pragma unroll
-        for (int c = 0; c < 8; ++c)
-            f[c] = fma(hg[c][3], h[3], fma(hg[c][2], h[2], fma(hg[c][1], h[1], hg[c][0] * h[0])));
+        for (int c = 0; c < 8; ++c) {
+            DfDot acc(df64(0.f, 0.f));
+#pragma unroll
+            for (int m = 0; m < 4; ++m) acc.add(hg[c][m], h[m]);
+            f[c] = acc.value();
+        }
         emit(dim, f);
     }
 }
