@@ -164,35 +164,35 @@ __device__ __forceinline__ df64 df_rsqrt(df64 a)
 
 // ---- conversions --------------------------------------------------------
 
-// double -> pair, integer operations only.  hi takes the 24 leading
-// significand bits (truncated), lo the next bits of the remaining 29
-// (normalised, truncated to 24): |v - (hi + lo)| < 2^-47 |v|.  Magnitudes
-// below 2^-74, where lo would leave the normal float range, keep hi only
-// (an error below 2^-98 absolute); zeros, infinities and NaNs map to
-// themselves.
+// double -> pair without the FP64 pipe.  hi takes the 24 leading
+// significand bits, lo the next 24 of the remaining 29, both truncated:
+// |v - (hi + lo)| < 2^-47 |v|.  For an exponent e of v (v = 1.f 2^e) the
+// float exponent field of hi is e + 127, which the bits 60..29 of v plus
+// 2^30 give directly (the low nine bits of v's biased exponent, minus 384,
+// modulo 2^32); lo is the 29-bit remainder r, signed, converted to float
+// rounding toward zero (its 24 leading bits) and scaled by 2^(e-52).
+// Magnitudes outside [2^-74, 2^128), where lo or hi would leave the normal
+// float range, keep hi only (an error below 2^-98 absolute): zeros,
+// infinities and NaNs map to themselves.
 __device__ __forceinline__ df64 to_df(double v)
 {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const unsigned w = (unsigned)(b >> 32);
-    const unsigned sign = w & 0x80000000u;
-    const int de = (int)((w >> 20) & 0x7ffu);
-    const int fe = de - 1023 + 127;
-    const unsigned mant = (unsigned)(b >> 29) & 0x7fffffu;
-    if (fe <= 52 || fe >= 255) {
-        // outside the split's range: the high word alone (FP32 truncation,
-        // signed zero below the float range, infinity above, NaN kept)
-        if (de == 0x7ff) return {__uint_as_float(sign | 0x7f800000u | (mant ? 0x400000u : 0u)), 0.f};
-        if (fe <= 0) return {__uint_as_float(sign), 0.f};
-        if (fe >= 255) return {__uint_as_float(sign | 0x7f800000u), 0.f};
-        return {__uint_as_float(sign | ((unsigned)fe << 23) | mant), 0.f};
+    const unsigned lo32 = (unsigned)__double2loint(v), hi32 = (unsigned)__double2hiint(v);
+    const unsigned sign = hi32 & 0x80000000u;
+    const unsigned de = (hi32 >> 20) & 0x7ffu;   // biased exponent, e + 1023
+    if (de - 949u <= 201u) {                     // e in [-74, 127]
+        const float hi = __uint_as_float((__funnelshift_r(lo32, hi32, 29) + 0x40000000u) | sign);
+        const int m = (int)hi32 >> 31;            // 0 or -1
+        const int r = (int)(((lo32 & 0x1fffffffu) ^ (unsigned)m) - (unsigned)m);   // +-remainder
+        return {hi, __int2float_rz(r) * __uint_as_float((de - 948u) << 23)};
     }
-    const float hi = __uint_as_float(sign | ((unsigned)fe << 23) | mant);
-    const unsigned r = (unsigned)b & 0x1fffffffu;   // the 29 bits below hi
-    if (r == 0u) return {hi, 0.f};
-    const int n = 31 - __clz((int)r);               // leading one of r, 0..28
-    const unsigned m = n >= 23 ? (r >> (n - 23)) : (r << (23 - n));
-    const int le = fe - 52 + n;                     // >= 1 for fe > 52
-    return {hi, __uint_as_float(sign | ((unsigned)le << 23) | (m & 0x7fffffu))};
+    // outside the split's range: the high word alone (FP32 truncation,
+    // signed zero below the float range, infinity above, NaN kept)
+    unsigned hb;
+    if (de >= 897u && de <= 1150u) hb = (__funnelshift_r(lo32, hi32, 29) + 0x40000000u) | sign;
+    else if (de < 897u) hb = sign;
+    else if (de == 0x7ffu && ((hi32 & 0xfffffu) | lo32) != 0u) hb = sign | 0x7fc00000u;
+    else hb = sign | 0x7f800000u;
+    return {__uint_as_float(hb), 0.f};
 }
 
 // float -> double with integer operations (normal floats and zeros exact;

@@ -8,25 +8,31 @@
 namespace lulesh {
 
 // ---- the EOS with its arithmetic in pairs --------------------------------
+// The EOS parameters that the pair arithmetic compares against, converted
+// once per element.
+struct EosCuts {
+    df64 p_cut, pmin, q_cut;
+    __device__ explicit EosCuts(const lulesh_params &P) : p_cut(to_df(P.p_cut)), pmin(to_df(P.pmin)), q_cut(to_df(P.q_cut)) {}
+};
+
 // CalcPressureForElems (:2384-2413): p = (2/3)(1 + compression) e with the
 // reference's cuts (p_zero: vnewc >= eosvmax, tested by the reference
 // whether or not the bound is switched on); bvc receives
-// (2/3)(1 + compression).
-__device__ __forceinline__ df64 eos_pressure_df(df64 &bvc, double e, df64 comp, bool p_zero,
-                                                const lulesh_params &P)
+// (2/3)(1 + compression).  e is the energy as a pair.
+__device__ __forceinline__ df64 eos_pressure_df(df64 &bvc, df64 e, df64 comp, bool p_zero, const EosCuts &cut)
 {
     bvc = df64(2.0 / 3.0) * (comp + df64(1.f, 0.f));
-    df64 p = bvc * to_df(e);
-    if (df_gt(to_df(P.p_cut), fabs(p))) p = df64(0.f, 0.f);
+    df64 p = bvc * e;
+    if (df_gt(cut.p_cut, fabs(p))) p = df64(0.f, 0.f);
     if (p_zero) p = df64(0.f, 0.f);
-    if (df_gt(to_df(P.pmin), p)) p = to_df(P.pmin);
+    if (df_gt(cut.pmin, p)) p = cut.pmin;
     return p;
 }
 
 // sqrt((pbvc e + vv^2 bvc p) / rho0) with the reference's floor (:2485-2493)
-__device__ __forceinline__ df64 sound_term_df(double e, df64 vv, df64 bvc, df64 p, double rho0, bool unit_rho0)
+__device__ __forceinline__ df64 sound_term_df(df64 e, df64 vv, df64 bvc, df64 p, double rho0, bool unit_rho0)
 {
-    df64 ssc = fma(df64(2.0 / 3.0), to_df(e), vv * vv * bvc * p);
+    df64 ssc = fma(df64(2.0 / 3.0), e, vv * vv * bvc * p);
     if (!unit_rho0) ssc = df_div(ssc, to_df(rho0));
     if (!df_gt(ssc, df64(.111111e-36))) return df64(.333333e-18);
     return ssc * df_rsqrt(ssc);
@@ -65,6 +71,7 @@ __device__ __forceinline__ double material_update_df(const Dom &d, int k, DevSca
     const double rho0 = P.refdens;
     const bool unit_rho0 = ikey(rho0) == ikey(1.0);
     const double emin = P.emin, e_cut = P.e_cut;
+    const EosCuts cut(P);
     df64 p_new(0.f, 0.f), q_new(0.f, 0.f), ssn(0.f, 0.f), bvc;
     double e_new = 0.0;
     for (int j = 0; j < rep; ++j) {
@@ -75,14 +82,14 @@ __device__ __forceinline__ double material_update_df(const Dom &d, int k, DevSca
             opaque_df(qlin); opaque_df(qquad);
         }
         const df64 one(1.f, 0.f);
-        const df64 dvc = to_df(delvc);
-        df64 compression = df_rcp(to_df(vnewc)) - one;
-        const df64 vchalf = to_df(vnewc) - df_scale(dvc, 0.5f);
+        const df64 dvc = to_df(delvc), vn = to_df(vnewc);
+        df64 compression = df_rcp(vn) - one;
+        const df64 vchalf = vn - df_scale(dvc, 0.5f);
         df64 comp_half = df_rcp(vchalf) - one;
         df64 vhalf = vchalf;
         if (has_vmin && le(vnewc, eosvmin)) {
             comp_half = compression;
-            vhalf = to_df(vnewc);
+            vhalf = vn;
         }
         const bool p_zero = ge(vnewc, eosvmax);
         const bool at_vmax = has_vmax && p_zero;
@@ -96,27 +103,30 @@ __device__ __forceinline__ double material_update_df(const Dom &d, int k, DevSca
 
         e_new = e_old + to_double(-df_scale(dvc * pq_old, 0.5f));
         if (lt(e_new, emin)) e_new = emin;
-        const df64 p_half = eos_pressure_df(bvc, e_new, comp_half, p_zero, P);
+        df64 e_df = to_df(e_new);
+        const df64 p_half = eos_pressure_df(bvc, e_df, comp_half, p_zero, cut);
         q_new = df64(0.f, 0.f);
-        if (!gt(delvc, 0.)) q_new = fma(sound_term_df(e_new, vhalf, bvc, p_half, rho0, unit_rho0), qlin, qquad);
+        if (!gt(delvc, 0.)) q_new = fma(sound_term_df(e_df, vhalf, bvc, p_half, rho0, unit_rho0), qlin, qquad);
         const df64 pq_half = p_half + q_new;
         e_new = e_new + to_double(df_scale(dvc * (df_mul_f(pq_old, 3.f) - df_mul_f(pq_half, 4.f)), 0.5f));
         if (abs_lt(e_new, e_cut)) e_new = 0.;
         if (lt(e_new, emin)) e_new = emin;
 
-        p_new = eos_pressure_df(bvc, e_new, compression, p_zero, P);
+        e_df = to_df(e_new);
+        p_new = eos_pressure_df(bvc, e_df, compression, p_zero, cut);
         df64 q_tilde(0.f, 0.f);
-        if (!gt(delvc, 0.)) q_tilde = fma(sound_term_df(e_new, to_df(vnewc), bvc, p_new, rho0, unit_rho0), qlin, qquad);
+        if (!gt(delvc, 0.)) q_tilde = fma(sound_term_df(e_df, vn, bvc, p_new, rho0, unit_rho0), qlin, qquad);
         const df64 combo = (df_mul_f(pq_old, 7.f) - df_mul_f(pq_half, 8.f)) + (p_new + q_tilde);
         e_new = e_new - to_double(combo * dvc * df64(1.0 / 6.0));
         if (abs_lt(e_new, e_cut)) e_new = 0.;
         if (lt(e_new, emin)) e_new = emin;
 
-        p_new = eos_pressure_df(bvc, e_new, compression, p_zero, P);
-        ssn = sound_term_df(e_new, to_df(vnewc), bvc, p_new, rho0, unit_rho0);
+        e_df = to_df(e_new);
+        p_new = eos_pressure_df(bvc, e_df, compression, p_zero, cut);
+        ssn = sound_term_df(e_df, vn, bvc, p_new, rho0, unit_rho0);
         if (le(delvc, 0.)) {
             q_new = fma(ssn, qlin, qquad);
-            if (df_gt(to_df(P.q_cut), fabs(q_new))) q_new = df64(0.f, 0.f);
+            if (df_gt(cut.q_cut, fabs(q_new))) q_new = df64(0.f, 0.f);
         }
         if (rep > 1) {
             consume(e_new); opaque_df(p_new); opaque_df(q_new); opaque_df(ssn);
