@@ -15,6 +15,14 @@ constexpr int kBlockNode = 256;
 
 inline int elem_block(const Dom &d) { return d.eblock ? d.eblock : kBlockElem; }
 inline int node_block(const Dom &d) { return d.nblock ? d.nblock : kBlockNode; }
+
+// The kinematics kernels (128 registers, two 256-thread blocks per SM
+// rather than four of 128: the same sixteen warps, but each SM sub-partition
+// runs two warps of one block, which start together and walk the long
+// straight-line body close to each other, so fewer warps wait on
+// instruction fetch): 4-6 % faster at s=192 in both arithmetics.
+constexpr int kKinBlockFactor = 2;
+inline int kin_block(const Dom &d) { return kKinBlockFactor * elem_block(d); }
 // Block sizes for a mesh of ne elements and nn nodes on a GPU with sms SMs:
 // the defaults, halved (down to one warp) while a kernel would have fewer
 // than four blocks per SM -- one FP64-bound element per thread makes the SM

@@ -431,8 +431,9 @@ __device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevSc
     gq[1 * ne + k] = vscale * dot3(c31, V2);                                  // delv_eta
 }
 
-// Four blocks per SM (128 registers, no spills: the pairs need them).
-__global__ void __launch_bounds__(kBlockElem, 4) k_elem_kinematics_split(const __grid_constant__ Dom d)
+// Two 256-thread blocks per SM (128 registers: the pairs need them; see
+// kin_block).
+__global__ void __launch_bounds__(kKinBlockFactor * kBlockElem, 2) k_elem_kinematics_split(const __grid_constant__ Dom d)
 {
     if (skip_step(d)) return;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -491,10 +492,11 @@ __device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScal
     }
 }
 
-// Six blocks per SM (85 registers: the EOS in pairs needs more than the 64
-// the FP64 one was held to).
+// Eight blocks per SM (64 registers, ~30 bytes spilled): the kernel waits on
+// its neighbour loads, and the extra warps hide them better than the spills
+// cost (0.61 ms at six blocks, 0.56 at seven, 0.55 at eight, s=192).
 template <bool kConstraints>
-__global__ void __launch_bounds__(kBlockElem, 6) k_elem_material_split(const __grid_constant__ Dom d)
+__global__ void __launch_bounds__(kBlockElem, 8) k_elem_material_split(const __grid_constant__ Dom d)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long kc = ~0ULL, kh = ~0ULL;
@@ -535,7 +537,7 @@ void launch_lagrange_nodal_split(const Dom &d, cudaStream_t st)
 
 void launch_lagrange_elements_split(const Dom &d, cudaStream_t st, bool with_constraints)
 {
-    k_elem_kinematics_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    k_elem_kinematics_split<<<blocks_for(d.ne, kin_block(d)), kin_block(d), 0, st>>>(d);
     if (with_constraints)
         k_elem_material_split<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     else
@@ -559,7 +561,7 @@ void launch_cycle_timed_split(const Dom &d, cudaStream_t st, cudaEvent_t ev[kTim
     cudaEventRecord(ev[2], st);
     k_node_update_split<<<blocks_for(d.nn, node_block(d)), node_block(d), 0, st>>>(d);
     cudaEventRecord(ev[3], st);
-    k_elem_kinematics_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
+    k_elem_kinematics_split<<<blocks_for(d.ne, kin_block(d)), kin_block(d), 0, st>>>(d);
     cudaEventRecord(ev[4], st);
     k_elem_material_split<true><<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     cudaEventRecord(ev[5], st);
