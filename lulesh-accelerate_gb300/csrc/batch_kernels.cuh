@@ -64,12 +64,13 @@ __global__ void kb_material(const __grid_constant__ Dom d, const __grid_constant
     kb_material_tiles<Body>(d, b, cls);
 }
 
-// Register-capped variants for the split-precision kinematics and material
-// bodies, which wait on their gathers: blocks of up to kBatchMaxBlock
-// threads (the autotuner's largest), kMinBlocks of them resident per SM, so
-// 4 -> 64 registers, 3 -> 85 and 2 -> 128.  On the 528-instance split
-// ensemble (kinematics at 128 registers instead of 134, material with its
-// FP64 EOS at 64 instead of 77) this took 36.7 s to 30.2 s; capping the
+// Register-capped variants for the kinematics and material bodies, which
+// wait on their gathers: blocks of up to kBatchMaxBlock threads (the
+// autotuner's largest), kMinBlocks of them resident per SM, so 4 -> 64
+// registers, 3 -> 85 and 2 -> 128.  The material bodies of both arithmetics
+// run at 64 (as the single-instance material kernels do).  On the
+// 528-instance split ensemble (kinematics at 128 registers instead of 134,
+// material at 64 instead of 77) this took 36.7 s to 30.2 s; capping the
 // force body as well (64 or 85 registers, with spills) lost 5 %.
 constexpr int kBatchMaxBlock = 256;
 

@@ -51,17 +51,19 @@ __device__ __forceinline__ void fb_hourglass_df(const Dom &d, const int nl[8], c
     }
     // One velocity component per iteration, the loop kept rolled: the body is
     // the same code three times over, and the smaller instruction footprint
-    // ran the force kernel 5 % faster at s=192 (2.09 -> 1.99 ms).
+    // ran the force kernel 5 % faster at s=192 (2.09 -> 1.99 ms).  Each
+    // iteration issues the next component's corner gather before its own
+    // arithmetic, so those loads are in flight while it computes
+    // (1.87 -> 1.82 ms; staging all 24 in shared memory at the start instead
+    // ran at 2.03).
+    double un[8];
+    gather8(d.xd, nl, un);
 #pragma unroll 1
     for (int dim = 0; dim < 3; ++dim) {
-        const double *vel = dim == 0 ? d.xd : (dim == 1 ? d.yd : d.zd);
         df64 u[8];
-        {
-            double ud[8];
-            gather8(vel, nl, ud);
 #pragma unroll
-            for (int c = 0; c < 8; ++c) u[c] = to_df(ud[c]);
-        }
+        for (int c = 0; c < 8; ++c) u[c] = to_df(un[c]);
+        if (dim < 2) gather8(dim == 0 ? d.yd : d.zd, nl, un);
         df64 h[4];
 #pragma unroll
         for (int m = 0; m < 4; ++m) {

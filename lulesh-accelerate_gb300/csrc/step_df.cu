@@ -443,7 +443,7 @@ void launch_batch_kernel_df(const Dom &d, const BatchView &b, cudaStream_t st, i
     case 0: kb_elem<elem_force_df><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     case 1: kb_node<node_update_df><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     case 2: kb_elem<elem_kinematics_df><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
-    default: kb_material<elem_material_df<true>><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    default: kb_material_capped<elem_material_df<true>, 4><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     }
 }
 
@@ -455,7 +455,7 @@ int batch_max_blocks_df(int kernel, int block)
     case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_force_df>, block, 0); break;
     case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_node<node_update_df>, block, 0); break;
     case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_kinematics_df>, block, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material<elem_material_df<true>>, block, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material_capped<elem_material_df<true>, 4>, block, 0); break;
     }
     return e == cudaSuccess ? n : 0;
 }

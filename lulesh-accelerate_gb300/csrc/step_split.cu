@@ -67,33 +67,6 @@ struct DF {
     float hi, lo;
 };
 
-// b - a for hi/lo pairs: Knuth's two-sum gives the exact difference of the
-// hi words as s + e; the lo words' difference is added to e.
-__device__ __forceinline__ DF df_diff(float2 b, float2 a)
-{
-    const float s = b.x - a.x;
-    const float bb = s - b.x;
-    const float e = (b.x - (s - bb)) - (a.x + bb);
-    return {s, e + (b.y - a.y)};
-}
-
-// a + b + c + d: exact two-sums on the hi words, the rest summed in FP32.
-__device__ __forceinline__ DF df_sum4(DF a, DF b, DF c, DF d)
-{
-    float s = a.hi, err = 0.f;
-    const float h[3] = {b.hi, c.hi, d.hi};
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const float t = s + h[i];
-        const float bb = t - s;
-        err += (s - (t - bb)) + (h[i] - bb);
-        s = t;
-    }
-    return {s, ((a.lo + b.lo) + (c.lo + d.lo)) + err};
-}
-
-__device__ __forceinline__ DF df_neg(DF a) { return {-a.hi, -a.lo}; }
-
 // hi + lo as the FP32 rounding of the sum and its exact remainder (Knuth's
 // two-sum), so that |lo| <= 2^-24 |hi|.
 __device__ __forceinline__ DF df_renorm(DF a)
@@ -103,28 +76,44 @@ __device__ __forceinline__ DF df_renorm(DF a)
     return {s, (a.hi - (s - bb)) + (a.lo - bb)};
 }
 
+// A value carried as h + e: h a float, e the exact rounding errors of the
+// sums that formed h plus the low words, gathered in one float.
+__device__ __forceinline__ DF bf_add(DF a, DF b)
+{
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    return {s, ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo)};
+}
+__device__ __forceinline__ DF bf_sub(DF a, DF b) { return bf_add(a, {-b.hi, -b.lo}); }
+
 // The Walsh modes M1..M6 of one coordinate of the 8 corners, from hi/lo
-// pairs, as renormalised hi/lo pairs.  Every mode but the constant one is a
-// signed sum of four edge differences (M1 = a+b+c+d, M4 = -a+b-c+d,
-// M5 = -a-b+c+d over the xi edges a..d; M2 = p+q+r+t, M6 = -p-q+r+t over the
-// eta edges; M3 over the zeta edges), so the sums run on small, exactly
-// formed differences in compensated FP32.  With linear_only, M1..M3 alone.
+// pairs, as renormalised hi/lo pairs: the three butterfly stages of walsh8
+// (hexmodes.cuh) with every high-word sum formed exactly (Knuth's two-sum)
+// and its error carried, with the low words, in the second float; one
+// renormalisation per mode.  With linear_only, M1..M3 alone.
 template <bool kLinearOnly>
 __device__ __forceinline__ void df_modes(const float2 *__restrict__ f, const int nl[8], DF m[6])
 {
-    float2 c[8];
+    DF c[8];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) c[i] = __ldg(f + nl[i]);
-    const DF a = df_diff(c[1], c[0]), b = df_diff(c[2], c[3]), cc = df_diff(c[5], c[4]), dd = df_diff(c[6], c[7]);
-    const DF p = df_diff(c[3], c[0]), q = df_diff(c[2], c[1]), r = df_diff(c[7], c[4]), t = df_diff(c[6], c[5]);
-    const DF u = df_diff(c[4], c[0]), v = df_diff(c[5], c[1]), w = df_diff(c[6], c[2]), z = df_diff(c[7], c[3]);
-    m[0] = df_renorm(df_sum4(a, b, cc, dd));
-    m[1] = df_renorm(df_sum4(p, q, r, t));
-    m[2] = df_renorm(df_sum4(u, v, w, z));
+    for (int i = 0; i < 8; ++i) {
+        const float2 v = __ldg(f + nl[i]);
+        c[i] = {v.x, v.y};
+    }
+    const DF s01 = bf_add(c[0], c[1]), d01 = bf_sub(c[1], c[0]);
+    const DF s32 = bf_add(c[3], c[2]), d32 = bf_sub(c[2], c[3]);
+    const DF s45 = bf_add(c[4], c[5]), d45 = bf_sub(c[5], c[4]);
+    const DF s76 = bf_add(c[7], c[6]), d76 = bf_sub(c[6], c[7]);
+    const DF dsm = bf_sub(s32, s01), dsp = bf_sub(s76, s45);   // eta differences of the zeta faces
+    const DF sdm = bf_add(d01, d32), sdp = bf_add(d45, d76);   // xi differences of the zeta faces
+    m[0] = df_renorm(bf_add(sdm, sdp));                          // xi
+    m[1] = df_renorm(bf_add(dsm, dsp));                          // eta
+    m[2] = df_renorm(bf_sub(bf_add(s45, s76), bf_add(s01, s32)));   // zeta
     if (!kLinearOnly) {
-        m[3] = df_renorm(df_sum4(df_neg(a), b, df_neg(cc), dd));
-        m[4] = df_renorm(df_sum4(df_neg(a), df_neg(b), cc, dd));
-        m[5] = df_renorm(df_sum4(df_neg(p), df_neg(q), r, t));
+        const DF ddm = bf_sub(d32, d01), ddp = bf_sub(d76, d45);
+        m[3] = df_renorm(bf_add(ddm, ddp));                      // xi eta
+        m[4] = df_renorm(bf_sub(sdp, sdm));                      // xi zeta
+        m[5] = df_renorm(bf_sub(dsp, dsm));                      // eta zeta
     }
 }
 
@@ -379,7 +368,7 @@ __device__ __forceinline__ void elem_kinematics_split(const Dom &d, int k, DevSc
     // through the Walsh modes of the corner coordinates and velocities
     // (CalcKinematicsForElems :1950-1958, :1975-2020, CalcElemCharacteristic-
     // Length :1821-1862; the identities of hexmodes.cuh).  The modes come
-    // from the hi/lo pairs by compensated FP32 edge sums (df_modes) as
+    // from the hi/lo pairs by an error-free FP32 butterfly (df_modes) as
     // hi + lo with |lo| <= 2^-24 |hi|, and the cross products, volume, strain
     // rate, face areas and divisions run on them as double-float pairs
     // (df64.cuh): FP64-grade (~2^-47) results without the FP64 pipe.  The
@@ -579,7 +568,7 @@ void launch_batch_kernel_split(const Dom &d, const BatchView &b, cudaStream_t st
     case 0: kb_elem<elem_force_split><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     case 1: kb_node<node_update_split><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     case 2: kb_elem_capped<elem_kinematics_split, 2><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
-    default: kb_material_capped<elem_material_split<true>, 3><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
+    default: kb_material_capped<elem_material_split<true>, 4><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     }
 }
 
@@ -592,7 +581,7 @@ int batch_max_blocks_split(int kernel, int block)
     case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem<elem_force_split>, block, 0); break;
     case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_node<node_update_split>, block, 0); break;
     case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_elem_capped<elem_kinematics_split, 2>, block, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material_capped<elem_material_split<true>, 3>, block, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_material_capped<elem_material_split<true>, 4>, block, 0); break;
     }
     return e == cudaSuccess ? n : 0;
 }
