@@ -387,9 +387,13 @@ int lulesh_batch_zone_cycles(lulesh_batch *b, double *zone_cycles);
 /* Choose threads per block (64/128/256, i.e. 4/2/1 elements per thread of a
  * 256-element tile) and resident blocks per SM (1/2/4/8) of each step kernel
  * per size class by timing the candidates on this batch, whose state is
- * restored afterwards.  Choices are cached in the JSON file cache_path
- * (keyed by GPU model, SM count, precision, class, kernel; NULL: no cache);
- * retune != 0 ignores cached entries. */
+ * restored afterwards; in split precision, for a class whose instances are
+ * all cubes with s >= 64, also the staging depth of the force kernel: its
+ * corners gathered from global memory (0), or tiles of 2 or 4 element rows
+ * x 64 columns staged in shared memory (blocks of 128 or 256 threads).
+ * Choices are cached in the JSON file cache_path (keyed by GPU model, SM
+ * count, precision, class, kernel; NULL: no cache); retune != 0 ignores
+ * cached entries. */
 int lulesh_batch_autotune(lulesh_batch *b, const char *cache_path, int retune);
 
 /* lulesh_batch_run in chunks of at most chunk cycles; after a chunk, when the
@@ -402,6 +406,15 @@ int lulesh_batch_autotune(lulesh_batch *b, const char *cache_path, int retune);
 int lulesh_batch_run_retuned(lulesh_batch *b, int chunk, double fraction, int max_cycles, int *cycles_done,
                              int *retunes);
 int lulesh_batch_tuning(lulesh_batch *b, int size_class, int kernel, int *block, int *grid);
+/* The staging depth in use for a class's kernel: element rows per staged
+ * tile, 0 for gathered corners (always 0 but for the split force kernel). */
+int lulesh_batch_staging(lulesh_batch *b, int size_class, int kernel, int *rows);
+/* Set a class's kernel launch shape by hand: threads per block (a multiple
+ * of 32, at most 256), resident blocks per SM of the persistent grid
+ * (>= 1, capped at what fits), staging depth rows (0; or 2 or 4 for the
+ * split force kernel of a class that can be staged, block then ignored).
+ * The shapes change no element's arithmetic. */
+int lulesh_batch_set_tuning(lulesh_batch *b, int size_class, int kernel, int block, int blocks_per_sm, int rows);
 
 void *lulesh_batch_stream(lulesh_batch *b);
 long long lulesh_batch_kernel_launches(lulesh_batch *b);

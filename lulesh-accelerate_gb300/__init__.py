@@ -167,6 +167,8 @@ _SIGNATURES = {
     "lulesh_batch_run_retuned": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int),
                                            C.POINTER(C.c_int)]),
     "lulesh_batch_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "lulesh_batch_staging": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "lulesh_batch_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     "lulesh_batch_stream": (C.c_void_p, [C.c_void_p]),
     "lulesh_batch_kernel_launches": (C.c_longlong, [C.c_void_p]),
 }
@@ -595,13 +597,22 @@ class Batch:
         _check_batch(load_library().lulesh_batch_autotune(self._h, path, int(retune)), self._h)
 
     def tuning(self) -> dict:
+        """Launch shape per class and kernel: threads per block, persistent
+        grid, and the staging depth (element rows per staged tile, 0 for
+        gathered corners)."""
         out = {}
         for cls in range(3):
             for k, name in enumerate(BATCH_KERNELS):
-                b, g = C.c_int(), C.c_int()
+                b, g, r = C.c_int(), C.c_int(), C.c_int()
                 load_library().lulesh_batch_tuning(self._h, cls, k, C.byref(b), C.byref(g))
-                out[f"class{cls}/{name}"] = {"block": b.value, "grid": g.value}
+                load_library().lulesh_batch_staging(self._h, cls, k, C.byref(r))
+                out[f"class{cls}/{name}"] = {"block": b.value, "grid": g.value, "stage": r.value}
         return out
+
+    def set_tuning(self, size_class: int, kernel: str, block: int = 128, blocks_per_sm: int = 4, rows: int = 0):
+        """Set one kernel's launch shape by hand (see lulesh_batch_set_tuning)."""
+        _check_batch(load_library().lulesh_batch_set_tuning(self._h, size_class, BATCH_KERNELS.index(kernel), block,
+                                                            blocks_per_sm, rows), self._h)
 
     @property
     def stream(self) -> int:

@@ -19,13 +19,16 @@
 // CUDA graph with a conditional WHILE node that loops while any instance is
 // active -- no host synchronisation per cycle.
 //
-// Launch shapes (threads per block = kTile / elements per thread, and
-// resident blocks per SM of the persistent grid) are chosen per size class
-// and kernel by lulesh_batch_autotune, which times the candidates on the
-// batch itself, restores its state, and caches the choice per GPU model.
+// Launch shapes (threads per block = kTile / elements per thread, resident
+// blocks per SM of the persistent grid, and for the split force kernel of a
+// class of structured cubes the staging depth: gathered corners, or tiles of
+// two or four element rows staged in shared memory) are chosen per size
+// class and kernel by lulesh_batch_autotune, which times the candidates on
+// the batch itself, restores its state, and caches the choice per GPU model.
 #include "lulesh_internal.h"
 #include "kernels.h"
 #include "common.cuh"
+#include "tile.cuh"
 
 #include <cuda_runtime.h>
 
@@ -51,6 +54,9 @@ struct lulesh_batch {
     int class_etiles[kMaxClasses] = {0, 0, 0};
     int class_ntiles[kMaxClasses] = {0, 0, 0};
     LaunchCfg cfg[kMaxClasses][kBatchKernels];
+    // staged tiles of the split force kernel, per class, for tiles of 2 and
+    // of 4 element rows (n == 0: the class cannot be staged)
+    StagedClass staged[kMaxClasses][2] = {};
     int sms = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t side[kMaxClasses] = {nullptr, nullptr, nullptr};
@@ -215,11 +221,30 @@ __global__ void kb_compact(const __grid_constant__ BatchView b)
 
 // ---- host helpers ------------------------------------------------------
 
+// Staging depths of the split force kernel (element rows per staged tile).
+const int kStageRows[2] = {2, 4};
+int stage_index(int rows) { return rows == 4 ? 1 : 0; }
+bool can_stage(const lulesh_batch *b, int cls)
+{
+    return b->precision == LULESH_PRECISION_SPLIT && b->staged[cls][0].n > 0;
+}
+
 void launch_kernel(lulesh_batch *b, int kernel, int cls, cudaStream_t st)
 {
     const LaunchCfg cfg = b->cfg[cls][kernel];
-    if (b->precision == LULESH_PRECISION_SPLIT) launch_batch_kernel_split(b->dom, b->bv, st, kernel, cls, cfg);
+    if (b->precision == LULESH_PRECISION_SPLIT && kernel == 0 && cfg.stage > 0 && can_stage(b, cls))
+        launch_batch_force_split_staged(b->dom, b->bv, b->staged[cls][stage_index(cfg.stage)], cfg.stage, cfg, st);
+    else if (b->precision == LULESH_PRECISION_SPLIT) launch_batch_kernel_split(b->dom, b->bv, st, kernel, cls, cfg);
     else launch_batch_kernel_fp64(b->dom, b->bv, st, kernel, cls, cfg);
+}
+
+// Staged tiles of the split force kernel over all of a class's instances.
+long long staged_tiles(const lulesh_batch *b, int cls, int rows)
+{
+    long long t = 0;
+    for (int i = 0; i < b->n; ++i)
+        if (b->inst_class[i] == cls) t += rows == 4 ? TileShape<4>::tiles(b->s[i]) : TileShape<2>::tiles(b->s[i]);
+    return t;
 }
 
 int max_blocks(lulesh_batch *b, int kernel, int block)
@@ -358,10 +383,15 @@ std::string tune_key(const lulesh_batch *b, int cls, int kernel)
     return o.str();
 }
 
-// The cache is a flat JSON object {"key": [block, blocks_per_sm], ...}.
-std::map<std::string, std::pair<int, int>> read_cache(const char *path)
+// The cache is a flat JSON object {"key": [block, blocks_per_sm, stage], ...}
+// (stage: element rows per staged tile, 0 for gathered corners; entries
+// without it read as 0).
+struct TuneEntry {
+    int block, per_sm, stage;
+};
+std::map<std::string, TuneEntry> read_cache(const char *path)
 {
-    std::map<std::string, std::pair<int, int>> m;
+    std::map<std::string, TuneEntry> m;
     std::ifstream f(path);
     if (!f) return m;
     std::stringstream ss;
@@ -374,21 +404,22 @@ std::map<std::string, std::pair<int, int>> read_cache(const char *path)
         const std::string key = t.substr(p + 1, q - p - 1);
         const size_t lb = t.find('[', q), rb = t.find(']', q);
         if (lb == std::string::npos || rb == std::string::npos) break;
-        int a = 0, c = 0;
-        if (sscanf(t.c_str() + lb + 1, "%d , %d", &a, &c) == 2) m[key] = {a, c};
+        int a = 0, c = 0, st = 0;
+        const int got = sscanf(t.c_str() + lb + 1, "%d , %d , %d", &a, &c, &st);
+        if (got >= 2) m[key] = {a, c, got == 3 ? st : 0};
         p = rb + 1;
     }
     return m;
 }
 
-void write_cache(const char *path, const std::map<std::string, std::pair<int, int>> &m)
+void write_cache(const char *path, const std::map<std::string, TuneEntry> &m)
 {
     std::ofstream f(path);
     f << "{\n";
     size_t i = 0;
     for (const auto &kv : m)
-        f << "  \"" << kv.first << "\": [" << kv.second.first << ", " << kv.second.second << "]"
-          << (++i < m.size() ? ",\n" : "\n");
+        f << "  \"" << kv.first << "\": [" << kv.second.block << ", " << kv.second.per_sm << ", "
+          << kv.second.stage << "]" << (++i < m.size() ? ",\n" : "\n");
     f << "}\n";
 }
 
@@ -511,6 +542,7 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
     unsigned char *nbc;
     double *volo, *emass, *nmass;
 #define A(p, cnt) if ((rc = balloc(b, &(p), (cnt))) != LULESH_OK) return bail(rc)
+#define A2(p, cnt) if ((rc = balloc(b, &(p), (cnt))) != LULESH_OK) return bail(rc)
     A(nodelist, 8 * ne); A(cstart, nn + 1); A(clist, 8 * ne); A(nbc, nn);
     A(lxim, ne); A(lxip, ne); A(letam, ne); A(letap, ne); A(lzetam, ne); A(lzetap, ne); A(ebc, ne);
     A(volo, ne); A(emass, ne); A(nmass, nn);
@@ -660,6 +692,44 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
         b->err = std::string("lulesh_batch_create upload: ") + cudaGetErrorString(cudaGetLastError());
         return bail(LULESH_ERR_CUDA);
     }
+    // the staged tiles of the split force kernel, for every class whose
+    // instances are all cubes of at least one tile row's width
+    if (precision == LULESH_PRECISION_SPLIT) {
+        for (int c = 0; c < kMaxClasses; ++c) {
+            std::vector<int> inst, sz, eb, nb;
+            bool all = true;
+            for (int i = 0; i < n; ++i)
+                if (b->inst_class[i] == c) {
+                    all = all && sizes[i] >= kTileCols;
+                    inst.push_back(i);
+                    sz.push_back(sizes[i]);
+                    eb.push_back((int)b->eoff[i]);
+                    nb.push_back((int)b->noff[i]);
+                }
+            if (inst.empty() || !all) continue;
+            const int m = (int)inst.size();
+            int *d_inst, *d_s, *d_eb, *d_nb;
+            A2(d_inst, m); A2(d_s, m); A2(d_eb, m); A2(d_nb, m);
+            ok = cudaMemcpy(d_inst, inst.data(), m * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+                 cudaMemcpy(d_s, sz.data(), m * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+                 cudaMemcpy(d_eb, eb.data(), m * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+                 cudaMemcpy(d_nb, nb.data(), m * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+            for (int r = 0; ok && r < 2; ++r) {
+                std::vector<long long> begin(m + 1, 0);
+                for (int j = 0; j < m; ++j)
+                    begin[j + 1] = begin[j] + (kStageRows[r] == 4 ? TileShape<4>::tiles(sz[j]) : TileShape<2>::tiles(sz[j]));
+                long long *d_begin;
+                A2(d_begin, m + 1);
+                ok = cudaMemcpy(d_begin, begin.data(), (m + 1) * sizeof(long long), cudaMemcpyHostToDevice) == cudaSuccess;
+                b->staged[c][r] = {m, d_inst, d_s, d_eb, d_nb, d_begin};
+            }
+            if (!ok) {
+                b->err = std::string("lulesh_batch_create staged tiles: ") + cudaGetErrorString(cudaGetLastError());
+                return bail(LULESH_ERR_CUDA);
+            }
+        }
+    }
+#undef A2
     default_cfg(b);
     *out = b;
     return LULESH_OK;
@@ -830,10 +900,38 @@ int lulesh_batch_tuning(lulesh_batch *b, int cls, int kernel, int *block, int *g
     return LULESH_OK;
 }
 
+int lulesh_batch_staging(lulesh_batch *b, int cls, int kernel, int *rows)
+{
+    if (!b || !rows || cls < 0 || cls >= kMaxClasses || kernel < 0 || kernel >= kBatchKernels) return LULESH_ERR_ARG;
+    *rows = b->cfg[cls][kernel].stage;
+    return LULESH_OK;
+}
+
+int lulesh_batch_set_tuning(lulesh_batch *b, int cls, int kernel, int block, int blocks_per_sm, int rows)
+{
+    if (!b || cls < 0 || cls >= kMaxClasses || kernel < 0 || kernel >= kBatchKernels || blocks_per_sm < 1)
+        return bfail(b, LULESH_ERR_ARG, "lulesh_batch_set_tuning: bad arguments");
+    const int tiles = kernel == 1 ? b->class_ntiles[cls] : b->class_etiles[cls];
+    if (rows != 0) {
+        if (kernel != 0 || (rows != 2 && rows != 4) || !can_stage(b, cls))
+            return bfail(b, LULESH_ERR_ARG, "lulesh_batch_set_tuning: this class's kernel cannot be staged that deep");
+        const int per_sm = std::max(1, std::min(blocks_per_sm, batch_max_blocks_split_staged(rows)));
+        b->cfg[cls][kernel] = {rows * kTileCols,
+                               (int)std::max(1LL, std::min(staged_tiles(b, cls, rows), (long long)b->sms * per_sm)), rows};
+    } else {
+        if (block < 32 || block > 256 || block % 32)
+            return bfail(b, LULESH_ERR_ARG, "lulesh_batch_set_tuning: block must be a multiple of 32 up to 256");
+        const int per_sm = std::max(1, std::min(blocks_per_sm, max_blocks(b, kernel, block)));
+        b->cfg[cls][kernel] = {block, std::max(1, std::min(std::max(tiles, 1), b->sms * per_sm))};
+    }
+    destroy_graph(b);   // the run graph bakes in the launch shapes
+    return LULESH_OK;
+}
+
 int lulesh_batch_autotune(lulesh_batch *b, const char *cache_path, int retune)
 {
     if (!b) return LULESH_ERR_ARG;
-    std::map<std::string, std::pair<int, int>> cache;
+    std::map<std::string, TuneEntry> cache;
     if (cache_path) cache = read_cache(cache_path);
     bool need = false;
     for (int c = 0; c < kMaxClasses; ++c)
@@ -842,8 +940,16 @@ int lulesh_batch_autotune(lulesh_batch *b, const char *cache_path, int retune)
             if (!tiles) continue;
             auto it = cache.find(tune_key(b, c, k));
             if (it == cache.end() || retune) { need = true; continue; }
-            const int per_sm = std::max(1, std::min(it->second.second, max_blocks(b, k, it->second.first)));
-            b->cfg[c][k] = {it->second.first, std::max(1, std::min(tiles, b->sms * per_sm))};
+            const TuneEntry &te = it->second;
+            if (k == 0 && (te.stage == 2 || te.stage == 4) && can_stage(b, c)) {
+                const int per_sm = std::max(1, std::min(te.per_sm, batch_max_blocks_split_staged(te.stage)));
+                b->cfg[c][k] = {te.stage * kTileCols,
+                                (int)std::max(1LL, std::min(staged_tiles(b, c, te.stage), (long long)b->sms * per_sm)),
+                                te.stage};
+            } else {
+                const int per_sm = std::max(1, std::min(te.per_sm, max_blocks(b, k, te.block)));
+                b->cfg[c][k] = {te.block, std::max(1, std::min(tiles, b->sms * per_sm))};
+            }
         }
     if (need) {
         // snapshot the evolving state; tuning runs real kernels on it
@@ -882,30 +988,42 @@ int lulesh_batch_autotune(lulesh_batch *b, const char *cache_path, int retune)
                 float best = 1e30f;
                 LaunchCfg best_cfg = b->cfg[c][k];
                 int best_depth = 1;
+                auto try_cfg = [&](LaunchCfg cfg, int dp) {
+                    b->cfg[c][k] = cfg;
+                    float t = 1e30f;
+                    for (int r = 0; r < 3; ++r) {
+                        cudaEventRecord(e0, b->stream);
+                        launch_kernel(b, k, c, b->stream);
+                        cudaEventRecord(e1, b->stream);
+                        cudaEventSynchronize(e1);
+                        float ms = 0.f;
+                        cudaEventElapsedTime(&ms, e0, e1);
+                        t = std::min(t, ms);
+                    }
+                    if (t < best) {
+                        best = t;
+                        best_cfg = cfg;
+                        best_depth = dp;
+                    }
+                };
                 for (int bs : blocks) {
                     const int cap = max_blocks(b, k, bs);
-                    for (int dp : depths) {
-                        if (dp > cap) continue;
-                        b->cfg[c][k] = {bs, std::max(1, std::min(tiles, b->sms * dp))};
-                        float t = 1e30f;
-                        for (int r = 0; r < 3; ++r) {
-                            cudaEventRecord(e0, b->stream);
-                            launch_kernel(b, k, c, b->stream);
-                            cudaEventRecord(e1, b->stream);
-                            cudaEventSynchronize(e1);
-                            float ms = 0.f;
-                            cudaEventElapsedTime(&ms, e0, e1);
-                            t = std::min(t, ms);
-                        }
-                        if (t < best) {
-                            best = t;
-                            best_cfg = b->cfg[c][k];
-                            best_depth = dp;
-                        }
-                    }
+                    for (int dp : depths)
+                        if (dp <= cap) try_cfg({bs, std::max(1, std::min(tiles, b->sms * dp))}, dp);
                 }
+                // the split force kernel of a class of structured cubes: the
+                // staged tiles, two or four element rows deep
+                if (k == 0 && can_stage(b, c))
+                    for (int rows : kStageRows) {
+                        const int cap = batch_max_blocks_split_staged(rows);
+                        const long long st_tiles = staged_tiles(b, c, rows);
+                        for (int dp : depths)
+                            if (dp <= cap)
+                                try_cfg({rows * kTileCols, (int)std::max(1LL, std::min(st_tiles, (long long)b->sms * dp)), rows},
+                                        dp);
+                    }
                 b->cfg[c][k] = best_cfg;
-                cache[tune_key(b, c, k)] = {best_cfg.block, best_depth};
+                cache[tune_key(b, c, k)] = {best_cfg.block, best_depth, best_cfg.stage};
             }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);

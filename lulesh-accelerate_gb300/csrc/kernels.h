@@ -80,5 +80,8 @@ void launch_batch_kernel_split(const Dom &d, const BatchView &b, cudaStream_t st
                                LaunchCfg cfg);
 int batch_max_blocks_fp64(int kernel, int block, int arith);
 int batch_max_blocks_split(int kernel, int block);
+void launch_batch_force_split_staged(const Dom &d, const BatchView &b, const StagedClass &sc, int rows,
+                                     LaunchCfg cfg, cudaStream_t st);
+int batch_max_blocks_split_staged(int rows);
 
 }  // namespace lulesh

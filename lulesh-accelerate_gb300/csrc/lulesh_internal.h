@@ -180,8 +180,27 @@ struct BatchView {
     unsigned char *inst_active;
 };
 
+// Launch shape of a batched kernel: threads per block, persistent grid, and
+// for the split force kernel of a class of structured cubes the staging
+// depth -- 0 gathers every element's corners from global memory, 2 or 4
+// stages tiles of that many element rows x kTileCols columns in shared
+// memory (block = rows x kTileCols threads).
 struct LaunchCfg {
     int block, grid;
+    int stage = 0;
+};
+
+// The staged tiles of one size class of a split batch whose instances are
+// all structured cubes wide enough for a tile row (s >= kTileCols): the
+// class's instances in order, with their edge lengths, first element and
+// node in the flat arrays, and tile_begin[j] the first tile of instance j
+// (n + 1 entries; the tile count per instance depends on the rows per
+// tile, so there is one StagedClass per depth).
+struct StagedClass {
+    int n;
+    const int *inst, *s;
+    const int *elem_base, *node_base;
+    const long long *tile_begin;
 };
 
 }  // namespace lulesh

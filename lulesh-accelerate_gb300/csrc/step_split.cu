@@ -149,13 +149,14 @@ struct GlobalCorners {
     __device__ void rel(int f, float out[8]) const { rel8(pair_field(d, f), nl, out); }
 };
 
+template <class Shape>
 struct TileCorners {
-    const float2 *tile;   // [6][kTileNodes]
+    const float2 *tile;   // [6][Shape::kNodes]
     int li[8];            // the corners' places in the tile, in the reference's corner order
-    __device__ TileCorners(const float2 *t, int rr, int cc) : tile(t) { tile_corners(rr, cc, li); }
+    __device__ TileCorners(const float2 *t, int rr, int cc) : tile(t) { Shape::corners(rr, cc, li); }
     __device__ void rel(int f, float out[8]) const
     {
-        const float2 *t = tile + f * kTileNodes;
+        const float2 *t = tile + f * Shape::kNodes;
         const float2 a0 = t[li[0]];
         out[0] = 0.f;
 #pragma unroll
@@ -276,17 +277,62 @@ __device__ __forceinline__ void elem_force_split(const Dom &d, int k, DevScalars
 // k_elem_force_split, so the same bits.  The skip decision is taken once
 // per block (an error word another block sets meanwhile must not split the
 // block at its barrier).
-__global__ void __launch_bounds__(kTileThreads, 8) k_elem_force_split_tiled(const __grid_constant__ Dom d)
+__global__ void __launch_bounds__(SoloTile::kThreads, 8) k_elem_force_split_tiled(const __grid_constant__ Dom d)
 {
-    __shared__ float2 tile[6 * kTileNodes];
+    __shared__ float2 tile[6 * SoloTile::kNodes];
     __shared__ int skip;
-    const TileCoord t = tile_coord(d.s);
+    const TileCoord t = SoloTile::coord(d.s, blockIdx.x);
     if (threadIdx.x == 0) skip = skip_step(d) ? 1 : 0;
-    load_tile(tile, d.s, t, 0, 6, [&](int f) { return pair_field(d, f); });
+    SoloTile::load(tile, d.s, t, 0, 0, 6, [&](int f) { return pair_field(d, f); });
     __syncthreads();
     int k, rr, cc;
-    if (skip || !tile_element(d.s, t, k, rr, cc)) return;
-    elem_force_split_from(d, k, d.sc, TileCorners(tile, rr, cc));
+    if (skip || !SoloTile::element(d.s, t, k, rr, cc)) return;
+    elem_force_split_from(d, k, d.sc, TileCorners<SoloTile>(tile, rr, cc));
+}
+
+// The staged force kernel over the structured cubes of one size class of a
+// batched ensemble (every instance of the class has s >= kTileCols): a
+// persistent grid walks the class's staged tiles, instance by instance
+// (StagedClass::tile_begin), skipping instances that have retired or
+// failed; each tile is staged and computed as in k_elem_force_split_tiled,
+// with the instance's element and node offsets and its own scalar block.
+// ROWS (2 or 4 element rows per tile of 64 columns) is the staging depth the
+// autotuner chooses.  The same arithmetic as the gathering batch kernel, so
+// the same bits.
+template <int ROWS>
+__global__ void __launch_bounds__(TileShape<ROWS>::kThreads, 1024 / TileShape<ROWS>::kThreads)
+    kb_force_split_staged(const __grid_constant__ Dom d, const __grid_constant__ BatchView b,
+                          const __grid_constant__ StagedClass sc)
+{
+    using Shape = TileShape<ROWS>;
+    __shared__ float2 tile[6 * Shape::kNodes];
+    __shared__ int s_j, s_skip;
+    const long long total = sc.tile_begin[sc.n];
+    for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+        if (threadIdx.x == 0) {
+            // the last instance whose first tile is at or before t
+            int lo = 0, hi = sc.n - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) / 2;
+                if (sc.tile_begin[mid] <= t) lo = mid;
+                else hi = mid - 1;
+            }
+            s_j = lo;
+            const int inst = sc.inst[lo];
+            s_skip = (!b.inst_active[inst] || d.sc[inst].err_any) ? 1 : 0;
+        }
+        __syncthreads();
+        if (!s_skip) {   // the same for the whole block
+            const int j = s_j, s = sc.s[j];
+            const TileCoord tc = Shape::coord(s, t - sc.tile_begin[j]);
+            Shape::load(tile, s, tc, sc.node_base[j], 0, 6, [&](int f) { return pair_field(d, f); });
+            __syncthreads();
+            int k, rr, cc;
+            if (Shape::element(s, tc, k, rr, cc))
+                elem_force_split_from(d, sc.elem_base[j] + k, d.sc + sc.inst[j], TileCorners<Shape>(tile, rr, cc));
+        }
+        __syncthreads();   // the tile and s_j are rewritten for the next tile
+    }
 }
 
 // The FP32 force kernel waits on its corner gathers rather than on an
@@ -507,7 +553,7 @@ static inline unsigned blocks_for(long n, int bs) { return (unsigned)((n + bs - 
 static void launch_elem_force_split(const Dom &d, cudaStream_t st)
 {
     if (d.s >= kTileCols) {
-        k_elem_force_split_tiled<<<(unsigned)tile_blocks(d.s), kTileThreads, 0, st>>>(d);
+        k_elem_force_split_tiled<<<(unsigned)SoloTile::tiles(d.s), SoloTile::kThreads, 0, st>>>(d);
     } else {
         k_elem_force_split<<<blocks_for(d.ne, elem_block(d)), elem_block(d), 0, st>>>(d);
     }
@@ -570,6 +616,24 @@ void launch_batch_kernel_split(const Dom &d, const BatchView &b, cudaStream_t st
     case 2: kb_elem_capped<elem_kinematics_split, 2><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     default: kb_material_capped<elem_material_split<true>, 4><<<cfg.grid, cfg.block, 0, st>>>(d, b, cls); break;
     }
+}
+
+// The staged batched force kernel of one class with `rows` element rows per
+// tile (cfg.block is then rows x kTileCols).
+void launch_batch_force_split_staged(const Dom &d, const BatchView &b, const StagedClass &sc, int rows,
+                                     LaunchCfg cfg, cudaStream_t st)
+{
+    if (rows == 4) kb_force_split_staged<4><<<cfg.grid, TileShape<4>::kThreads, 0, st>>>(d, b, sc);
+    else kb_force_split_staged<2><<<cfg.grid, TileShape<2>::kThreads, 0, st>>>(d, b, sc);
+}
+
+int batch_max_blocks_split_staged(int rows)
+{
+    int n = 0;
+    const cudaError_t e =
+        rows == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_force_split_staged<4>, TileShape<4>::kThreads, 0)
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_force_split_staged<2>, TileShape<2>::kThreads, 0);
+    return e == cudaSuccess ? n : 0;
 }
 
 // Resident blocks per SM of a batched kernel at a block size.

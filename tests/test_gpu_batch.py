@@ -122,3 +122,60 @@ def test_retuned_run_equals_plain_run(pkg, precision):
             for k in ("x", "xd", "e", "p", "q", "v", "ss"):
                 assert np.array_equal(a.get_field(i, k), b.get_field(i, k)), (i, k)
 
+
+
+def test_staged_force_equals_gathered_in_batch(pkg):
+    """The staging depth of the split force kernel (corners gathered, or
+    tiles of 2 or 4 element rows staged in shared memory) changes no bit:
+    a class of cubes with s >= 64, among them sizes that leave partial tiles
+    (66: a partial row pair and column block, 70), run at each depth."""
+    sizes, scale = [64, 66, 70], [1.0, 0.8, 1.3]
+    results = {}
+    for rows in (0, 2, 4):
+        with pkg.Batch(sizes, scale, pkg.INIT_V2, pkg.SPLIT) as b:
+            b.set_tuning(2, "elem_force", block=128, blocks_per_sm=4, rows=rows)
+            assert b.tuning()["class2/elem_force"]["stage"] == rows
+            b.run(40)
+            results[rows] = [[b.get_field(i, k) for k in ("x", "xd", "e", "p", "q", "v", "ss")]
+                             for i in range(len(sizes))]
+            assert all(b.instance(i)[0].cycle == 40 for i in range(len(sizes)))
+    for rows in (2, 4):
+        for i in range(len(sizes)):
+            for a, c in zip(results[0][i], results[rows][i]):
+                assert np.array_equal(a, c), (rows, i)
+
+
+def test_staging_needs_a_class_of_wide_cubes(pkg):
+    """A class holding an instance narrower than a tile row (s < 64) cannot be
+    staged; asking for it is an argument error, and so is staging another
+    kernel or an FP64 batch."""
+    with pkg.Batch([50, 64], [1.0, 1.0], pkg.INIT_V2, pkg.SPLIT) as b:
+        with pytest.raises(pkg.LuleshError):
+            b.set_tuning(2, "elem_force", rows=2)
+        assert b.tuning()["class2/elem_force"]["stage"] == 0
+    with pkg.Batch([64], [1.0], pkg.INIT_V2, pkg.SPLIT) as b:
+        with pytest.raises(pkg.LuleshError):
+            b.set_tuning(2, "elem_kinematics", rows=2)
+        b.set_tuning(2, "elem_force", rows=4)
+    with pkg.Batch([64], [1.0], pkg.INIT_V2, pkg.FP64) as b:
+        with pytest.raises(pkg.LuleshError):
+            b.set_tuning(0, "elem_force", rows=2)
+
+
+def test_autotune_considers_staging(pkg, tmp_path):
+    """The autotuner times the staged depths for a class of wide cubes and
+    records the depth it chose with the shape; a cached choice is restored
+    with its depth."""
+    cache = tmp_path / "tuning.json"
+    with pkg.Batch([64, 65], [1.0, 1.1], pkg.INIT_V2, pkg.SPLIT) as b:
+        b.autotune(str(cache))
+        t = b.tuning()["class2/elem_force"]
+        assert t["stage"] in (0, 2, 4)
+        if t["stage"]:
+            assert t["block"] == 64 * t["stage"]
+    entries = json.loads(cache.read_text())
+    force = [v for k, v in entries.items() if k.endswith("class2|elem_force")]
+    assert force and len(force[0]) == 3 and force[0][2] == t["stage"]
+    with pkg.Batch([64, 65], [1.0, 1.1], pkg.INIT_V2, pkg.SPLIT) as c:
+        c.autotune(str(cache))
+        assert c.tuning()["class2/elem_force"] == t
