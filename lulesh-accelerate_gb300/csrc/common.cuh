@@ -172,6 +172,25 @@ __device__ __forceinline__ void node_integrate(const Dom &d, int n, const DevSca
     t = d.zd[n] + az * dt; if (abs_lt(t, u_cut)) t = 0.0; d.zd[n] = t; d.z[n] += t * dt;
 }
 
+// The six face neighbours of element k (lxim, lxip, letam, letap, lzetam,
+// lzetap).  On the structured s^3 cube of the reference's set-up
+// (Dom::s > 0) they are k -+ 1, k -+ s and k -+ s^2 across every interior
+// face, the only faces whose neighbour the limiter reads (a boundary face
+// carries a BC flag), so there they are formed instead of loaded: the
+// limiter's neighbour slopes then depend on no earlier load.
+struct FaceNeighbours {
+    int xim, xip, etam, etap, zetam, zetap;
+};
+__device__ __forceinline__ FaceNeighbours face_neighbours(const Dom &d, int k)
+{
+    if (d.s > 0) {
+        const int s = d.s, s2 = s * s;
+        return {k - 1, k + 1, k - s, k + s, k - s2, k + s2};
+    }
+    return {__ldg(d.lxim + k), __ldg(d.lxip + k), __ldg(d.letam + k),
+            __ldg(d.letap + k), __ldg(d.lzetam + k), __ldg(d.lzetap + k)};
+}
+
 // One direction of the monotonic limiter (:2198-2228).
 template <typename T>
 __device__ __forceinline__ T limiter_phi(const T *__restrict__ delv, int i, int bm, int bp,

@@ -354,15 +354,16 @@ __device__ __forceinline__ void elem_material_df(const Dom &d, int k, DevScalars
 {
     const lulesh_params &P = d.prm;
     const int bc = __ldg(d.elem_bc + k);
+    const FaceNeighbours nb = face_neighbours(d, k);
     const df64 lim = to_df(P.monoq_limiter_mult), maxs = to_df(P.monoq_max_slope);
     const df64 phixi = limiter_phi_df(d.delv_xi, k, bc & BC_XI_M, bc & BC_XI_P, BC_XI_M_SYMM, BC_XI_M_FREE,
-                                      BC_XI_P_SYMM, BC_XI_P_FREE, __ldg(d.lxim + k), __ldg(d.lxip + k), lim, maxs);
+                                      BC_XI_P_SYMM, BC_XI_P_FREE, nb.xim, nb.xip, lim, maxs);
     const df64 phieta = limiter_phi_df(d.delv_eta, k, bc & BC_ETA_M, bc & BC_ETA_P, BC_ETA_M_SYMM, BC_ETA_M_FREE,
-                                       BC_ETA_P_SYMM, BC_ETA_P_FREE, __ldg(d.letam + k), __ldg(d.letap + k), lim,
+                                       BC_ETA_P_SYMM, BC_ETA_P_FREE, nb.etam, nb.etap, lim,
                                        maxs);
     const df64 phizeta = limiter_phi_df(d.delv_zeta, k, bc & BC_ZETA_M, bc & BC_ZETA_P, BC_ZETA_M_SYMM,
-                                        BC_ZETA_M_FREE, BC_ZETA_P_SYMM, BC_ZETA_P_FREE, __ldg(d.lzetam + k),
-                                        __ldg(d.lzetap + k), lim, maxs);
+                                        BC_ZETA_M_FREE, BC_ZETA_P_SYMM, BC_ZETA_P_FREE, nb.zetam,
+                                        nb.zetap, lim, maxs);
     const double vnew = d.vnew[k], vdov = d.vdov[k];
     df64 qlin(0.f, 0.f), qquad(0.f, 0.f);
     if (!gt(vdov, 0.)) {

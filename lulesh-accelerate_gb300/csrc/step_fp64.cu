@@ -355,16 +355,17 @@ __device__ __forceinline__ void elem_material_fp64(const Dom &d, int k, DevScala
     {
         // CalcMonotonicQRegionForElems (:2182-2320)
         const int bc = __ldg(d.elem_bc + k);
+        const FaceNeighbours nb = face_neighbours(d, k);
         const double lim = P.monoq_limiter_mult, maxs = P.monoq_max_slope;
         const double phixi = limiter_phi(d.delv_xi, k, bc & BC_XI_M, bc & BC_XI_P, BC_XI_M_SYMM,
                                          BC_XI_M_FREE, BC_XI_P_SYMM, BC_XI_P_FREE,
-                                         __ldg(d.lxim + k), __ldg(d.lxip + k), lim, maxs);
+                                         nb.xim, nb.xip, lim, maxs);
         const double phieta = limiter_phi(d.delv_eta, k, bc & BC_ETA_M, bc & BC_ETA_P, BC_ETA_M_SYMM,
                                           BC_ETA_M_FREE, BC_ETA_P_SYMM, BC_ETA_P_FREE,
-                                          __ldg(d.letam + k), __ldg(d.letap + k), lim, maxs);
+                                          nb.etam, nb.etap, lim, maxs);
         const double phizeta = limiter_phi(d.delv_zeta, k, bc & BC_ZETA_M, bc & BC_ZETA_P,
                                            BC_ZETA_M_SYMM, BC_ZETA_M_FREE, BC_ZETA_P_SYMM,
-                                           BC_ZETA_P_FREE, __ldg(d.lzetam + k), __ldg(d.lzetap + k),
+                                           BC_ZETA_P_FREE, nb.zetam, nb.zetap,
                                            lim, maxs);
         const double vnew = d.vnew[k], volo = d.volo[k], vdov = d.vdov[k];
         double qlin, qquad;

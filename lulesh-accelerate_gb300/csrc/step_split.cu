@@ -488,16 +488,17 @@ __device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScal
         const size_t ne = (size_t)d.ne;
         const float *dv_xi = d.gq, *dv_eta = d.gq + ne, *dv_zeta = d.gq + 2 * ne;
         const int bc = __ldg(d.elem_bc + k);
+        const FaceNeighbours nb = face_neighbours(d, k);
         const float lim = d2f(P.monoq_limiter_mult), maxs = d2f(P.monoq_max_slope);
         const float phixi = limiter_phi<float>(dv_xi, k, bc & BC_XI_M, bc & BC_XI_P, BC_XI_M_SYMM,
                                                BC_XI_M_FREE, BC_XI_P_SYMM, BC_XI_P_FREE,
-                                               __ldg(d.lxim + k), __ldg(d.lxip + k), lim, maxs);
+                                               nb.xim, nb.xip, lim, maxs);
         const float phieta = limiter_phi<float>(dv_eta, k, bc & BC_ETA_M, bc & BC_ETA_P, BC_ETA_M_SYMM,
                                                 BC_ETA_M_FREE, BC_ETA_P_SYMM, BC_ETA_P_FREE,
-                                                __ldg(d.letam + k), __ldg(d.letap + k), lim, maxs);
+                                                nb.etam, nb.etap, lim, maxs);
         const float phizeta = limiter_phi<float>(dv_zeta, k, bc & BC_ZETA_M, bc & BC_ZETA_P,
                                                  BC_ZETA_M_SYMM, BC_ZETA_M_FREE, BC_ZETA_P_SYMM,
-                                                 BC_ZETA_P_FREE, __ldg(d.lzetam + k), __ldg(d.lzetap + k),
+                                                 BC_ZETA_P_FREE, nb.zetam, nb.zetap,
                                                  lim, maxs);
         const double vnew = d.vnew[k], vdov = d.vdov[k];
         float qlin = 0.f, qquad = 0.f;
