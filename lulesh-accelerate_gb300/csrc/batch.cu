@@ -644,6 +644,7 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
         h.courant_key = ~0ULL;
         h.hydro_key = ~0ULL;
         h.elem_begin = (int)eo_i;
+        h.edge = sizes[i];
         iee_h[i] = (int)(eo_i + nei);
         ine_h[i] = (int)(no_i + nni);
         cpos += 8 * nei;

@@ -173,18 +173,20 @@ __device__ __forceinline__ void node_integrate(const Dom &d, int n, const DevSca
 }
 
 // The six face neighbours of element k (lxim, lxip, letam, letap, lzetam,
-// lzetap).  On the structured s^3 cube of the reference's set-up
-// (Dom::s > 0) they are k -+ 1, k -+ s and k -+ s^2 across every interior
-// face, the only faces whose neighbour the limiter reads (a boundary face
-// carries a BC flag), so there they are formed instead of loaded: the
-// limiter's neighbour slopes then depend on no earlier load.
+// lzetap).  On the structured s^3 cube of the reference's set-up (Dom::s > 0,
+// or a batch instance's DevScalars::edge > 0, whose elements are contiguous)
+// they are k -+ 1, k -+ s and k -+ s^2 across every interior face, the only
+// faces whose neighbour the limiter reads (a boundary face carries a BC
+// flag), so there they are formed instead of loaded: the limiter's
+// neighbour slopes then depend on no earlier load.
 struct FaceNeighbours {
     int xim, xip, etam, etap, zetam, zetap;
 };
-__device__ __forceinline__ FaceNeighbours face_neighbours(const Dom &d, int k)
+__device__ __forceinline__ FaceNeighbours face_neighbours(const Dom &d, const DevScalars *sc, int k)
 {
-    if (d.s > 0) {
-        const int s = d.s, s2 = s * s;
+    const int s = d.s > 0 ? d.s : sc->edge;
+    if (s > 0) {
+        const int s2 = s * s;
         return {k - 1, k + 1, k - s, k + s, k - s2, k + s2};
     }
     return {__ldg(d.lxim + k), __ldg(d.lxip + k), __ldg(d.letam + k),

@@ -8,8 +8,9 @@
 namespace lulesh {
 
 // Threads per block of the element and node kernels.  The element kernels
-// are FP64-issue-bound; 128 threads keep the FP64 pipe busy with two to
-// four resident blocks per SM at their register counts.
+// are bound by instruction issue at 64-168 registers; 128 threads give two
+// to eight resident blocks per SM at their register counts (the kinematics
+// kernels run two such blocks' worth as one, see kin_block).
 constexpr int kBlockElem = 128;
 constexpr int kBlockNode = 256;
 

@@ -354,7 +354,7 @@ __device__ __forceinline__ void elem_material_df(const Dom &d, int k, DevScalars
 {
     const lulesh_params &P = d.prm;
     const int bc = __ldg(d.elem_bc + k);
-    const FaceNeighbours nb = face_neighbours(d, k);
+    const FaceNeighbours nb = face_neighbours(d, sc, k);
     const df64 lim = to_df(P.monoq_limiter_mult), maxs = to_df(P.monoq_max_slope);
     const df64 phixi = limiter_phi_df(d.delv_xi, k, bc & BC_XI_M, bc & BC_XI_P, BC_XI_M_SYMM, BC_XI_M_FREE,
                                       BC_XI_P_SYMM, BC_XI_P_FREE, nb.xim, nb.xip, lim, maxs);

@@ -355,7 +355,7 @@ __device__ __forceinline__ void elem_material_fp64(const Dom &d, int k, DevScala
     {
         // CalcMonotonicQRegionForElems (:2182-2320)
         const int bc = __ldg(d.elem_bc + k);
-        const FaceNeighbours nb = face_neighbours(d, k);
+        const FaceNeighbours nb = face_neighbours(d, sc, k);
         const double lim = P.monoq_limiter_mult, maxs = P.monoq_max_slope;
         const double phixi = limiter_phi(d.delv_xi, k, bc & BC_XI_M, bc & BC_XI_P, BC_XI_M_SYMM,
                                          BC_XI_M_FREE, BC_XI_P_SYMM, BC_XI_P_FREE,

@@ -488,7 +488,7 @@ __device__ __forceinline__ void elem_material_split(const Dom &d, int k, DevScal
         const size_t ne = (size_t)d.ne;
         const float *dv_xi = d.gq, *dv_eta = d.gq + ne, *dv_zeta = d.gq + 2 * ne;
         const int bc = __ldg(d.elem_bc + k);
-        const FaceNeighbours nb = face_neighbours(d, k);
+        const FaceNeighbours nb = face_neighbours(d, sc, k);
         const float lim = d2f(P.monoq_limiter_mult), maxs = d2f(P.monoq_max_slope);
         const float phixi = limiter_phi<float>(dv_xi, k, bc & BC_XI_M, bc & BC_XI_P, BC_XI_M_SYMM,
                                                BC_XI_M_FREE, BC_XI_P_SYMM, BC_XI_P_FREE,
