@@ -922,7 +922,9 @@ int lulesh_batch_set_tuning(lulesh_batch *b, int cls, int kernel, int block, int
     } else {
         if (block < 32 || block > 256 || block % 32)
             return bfail(b, LULESH_ERR_ARG, "lulesh_batch_set_tuning: block must be a multiple of 32 up to 256");
-        const int per_sm = std::max(1, std::min(blocks_per_sm, max_blocks(b, kernel, block)));
+        const int fit = max_blocks(b, kernel, block);
+        if (fit < 1) return bfail(b, LULESH_ERR_ARG, "lulesh_batch_set_tuning: no block of that size fits on an SM");
+        const int per_sm = std::min(blocks_per_sm, fit);
         b->cfg[cls][kernel] = {block, std::max(1, std::min(std::max(tiles, 1), b->sms * per_sm))};
     }
     destroy_graph(b);   // the run graph bakes in the launch shapes
