@@ -385,12 +385,13 @@ int lulesh_batch_get_field(lulesh_batch *b, int i, const char *name, double *hos
 int lulesh_batch_zone_cycles(lulesh_batch *b, double *zone_cycles);
 
 /* Choose threads per block (64/128/256, i.e. 4/2/1 elements per thread of a
- * 256-element tile) and resident blocks per SM (1/2/4/8) of each step kernel
- * per size class by timing the candidates on this batch, whose state is
- * restored afterwards; in split precision, for a class whose instances are
- * all cubes with s >= 64, also the staging depth of the force kernel: its
- * corners gathered from global memory (0), or tiles of 2 or 4 element rows
- * x 64 columns staged in shared memory (blocks of 128 or 256 threads).
+ * 256-element tile) and resident blocks per SM (1/2/4/8 and the most that
+ * fit) of each step kernel per size class by timing the candidates on this
+ * batch, whose state is restored afterwards; in split precision, for a
+ * class whose instances are all cubes with s >= 64, also the staging depth
+ * of the force kernel: its corners gathered from global memory (0), or
+ * tiles of 2 or 4 element rows x 64 columns staged in shared memory (blocks
+ * of 128 or 256 threads).
  * Choices are cached in the JSON file cache_path (keyed by GPU model, SM
  * count, precision, class, kernel; NULL: no cache); retune != 0 ignores
  * cached entries. */

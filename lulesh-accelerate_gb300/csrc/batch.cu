@@ -1009,21 +1009,27 @@ int lulesh_batch_autotune(lulesh_batch *b, const char *cache_path, int retune)
                         best_depth = dp;
                     }
                 };
-                for (int bs : blocks) {
-                    const int cap = max_blocks(b, k, bs);
+                // resident blocks per SM: 1, 2, 4, 8 and the most that fit
+                // (three 128-thread blocks of the 168-register force body,
+                // for instance, which no power of two reaches)
+                auto per_sm_candidates = [&](int cap) {
+                    std::vector<int> v;
                     for (int dp : depths)
-                        if (dp <= cap) try_cfg({bs, std::max(1, std::min(tiles, b->sms * dp))}, dp);
-                }
+                        if (dp <= cap) v.push_back(dp);
+                    if (cap >= 1 && std::find(v.begin(), v.end(), cap) == v.end()) v.push_back(cap);
+                    return v;
+                };
+                for (int bs : blocks)
+                    for (int dp : per_sm_candidates(max_blocks(b, k, bs)))
+                        try_cfg({bs, std::max(1, std::min(tiles, b->sms * dp))}, dp);
                 // the split force kernel of a class of structured cubes: the
                 // staged tiles, two or four element rows deep
                 if (k == 0 && can_stage(b, c))
                     for (int rows : kStageRows) {
-                        const int cap = batch_max_blocks_split_staged(rows);
                         const long long st_tiles = staged_tiles(b, c, rows);
-                        for (int dp : depths)
-                            if (dp <= cap)
-                                try_cfg({rows * kTileCols, (int)std::max(1LL, std::min(st_tiles, (long long)b->sms * dp)), rows},
-                                        dp);
+                        for (int dp : per_sm_candidates(batch_max_blocks_split_staged(rows)))
+                            try_cfg({rows * kTileCols, (int)std::max(1LL, std::min(st_tiles, (long long)b->sms * dp)), rows},
+                                    dp);
                     }
                 b->cfg[c][k] = best_cfg;
                 cache[tune_key(b, c, k)] = {best_cfg.block, best_depth, best_cfg.stage};
