@@ -10,9 +10,11 @@ namespace lulesh {
 // Threads per block of the element and node kernels.  The element kernels
 // are bound by instruction issue at 64-168 registers; 128 threads give two
 // to eight resident blocks per SM at their register counts (the kinematics
-// kernels run two such blocks' worth as one, see kin_block).
+// kernels run two such blocks' worth as one, see kin_block).  The node
+// updates, gathers bound by memory, ran 1-2 % faster in 128-thread blocks
+// than in 256 (512: 2-3 % slower).
 constexpr int kBlockElem = 128;
-constexpr int kBlockNode = 256;
+constexpr int kBlockNode = 128;
 
 inline int elem_block(const Dom &d) { return d.eblock ? d.eblock : kBlockElem; }
 inline int node_block(const Dom &d) { return d.nblock ? d.nblock : kBlockNode; }
