@@ -542,7 +542,6 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
     unsigned char *nbc;
     double *volo, *emass, *nmass;
 #define A(p, cnt) if ((rc = balloc(b, &(p), (cnt))) != LULESH_OK) return bail(rc)
-#define A2(p, cnt) if ((rc = balloc(b, &(p), (cnt))) != LULESH_OK) return bail(rc)
     A(nodelist, 8 * ne); A(cstart, nn + 1); A(clist, 8 * ne); A(nbc, nn);
     A(lxim, ne); A(lxip, ne); A(letam, ne); A(letap, ne); A(lzetam, ne); A(lzetap, ne); A(ebc, ne);
     A(volo, ne); A(emass, ne); A(nmass, nn);
@@ -567,7 +566,6 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
     A(iee, n); A(ine, n); A(eco, kMaxClasses); A(nco, kMaxClasses);
     A(b->bv.active_etiles, net); A(b->bv.active_ntiles, nnt); A(b->bv.counts, 2 * kMaxClasses + 2);
     A(b->bv.inst_active, n);
-#undef A
     d.nodelist = nodelist; d.corner_start = cstart; d.corner_list = clist; d.node_bc = nbc;
     d.lxim = lxim; d.lxip = lxip; d.letam = letam; d.letap = letap; d.lzetam = lzetam; d.lzetap = lzetap;
     d.elem_bc = ebc; d.volo = volo; d.elem_mass = emass; d.nodal_mass = nmass;
@@ -710,7 +708,7 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
             if (inst.empty() || !all) continue;
             const int m = (int)inst.size();
             int *d_inst, *d_s, *d_eb, *d_nb;
-            A2(d_inst, m); A2(d_s, m); A2(d_eb, m); A2(d_nb, m);
+            A(d_inst, m); A(d_s, m); A(d_eb, m); A(d_nb, m);
             ok = cudaMemcpy(d_inst, inst.data(), m * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
                  cudaMemcpy(d_s, sz.data(), m * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
                  cudaMemcpy(d_eb, eb.data(), m * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
@@ -720,7 +718,7 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
                 for (int j = 0; j < m; ++j)
                     begin[j + 1] = begin[j] + (kStageRows[r] == 4 ? TileShape<4>::tiles(sz[j]) : TileShape<2>::tiles(sz[j]));
                 long long *d_begin;
-                A2(d_begin, m + 1);
+                A(d_begin, m + 1);
                 ok = cudaMemcpy(d_begin, begin.data(), (m + 1) * sizeof(long long), cudaMemcpyHostToDevice) == cudaSuccess;
                 b->staged[c][r] = {m, d_inst, d_s, d_eb, d_nb, d_begin};
             }
@@ -730,7 +728,7 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
             }
         }
     }
-#undef A2
+#undef A
     default_cfg(b);
     *out = b;
     return LULESH_OK;
