@@ -109,6 +109,9 @@ __device__ __forceinline__ void load_geometry_df(const double *__restrict__ geo,
 __device__ __forceinline__ void elem_force_df(const Dom &d, int k, DevScalars *sc)
 {
     const size_t ne = (size_t)d.ne;
+    // the element scalars first: their loads are in flight with the geometry's
+    const double pk = __ldg(d.p + k), qk = __ldg(d.q + k), vk = __ldg(d.v + k), volok = __ldg(d.volo + k);
+    const double ssk = __ldg(d.ss + k), massk = __ldg(d.elem_mass + k);
     int nl[8];
     load_nodelist(d.nodelist, k, nl);
     // the modes and shared cross products: kept by the previous cycle's
@@ -137,7 +140,7 @@ __device__ __forceinline__ void elem_force_df(const Dom &d, int k, DevScalars *s
     // the Jacobian volume M2.(M3 x M1)/64 is tested.
     df64 Y[3][3];
     {
-        const df64 w = to_df((1.0 / 64.0) * (d.p[k] + d.q[k]));
+        const df64 w = to_df((1.0 / 64.0) * (pk + qk));
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             Y[i][0] = w * nx[i].x;
@@ -166,8 +169,7 @@ __device__ __forceinline__ void elem_force_df(const Dom &d, int k, DevScalars *s
     };
 
     // CalcHourglassControlForElems (:1503-1558)
-    const double vk = d.v[k];
-    const double determ = d.volo[k] * vk;
+    const double determ = volok * vk;
     if (vk <= 0.0) flag_error(sc, ERR_K1_VOLUME, k);
 
     const double hourg = d.prm.hgcoef;
@@ -187,7 +189,7 @@ __device__ __forceinline__ void elem_force_df(const Dom &d, int k, DevScalars *s
     const double r = rcbrt_fast(determ);                    // determ^(-1/3)
     const V3<df64> H[4] = {M6, M5, M4, mode(mx, my, mz, 6)};
     fb_hourglass_df(d, nl, dvdx, dvdy, dvdz, H, to_df((r * r * r) * (1.0 / 192.0)),
-                    to_df(-hourg * 0.01 * d.ss[k] * d.elem_mass[k] * r), [&](int dim, const df64 hgf[8]) {
+                    to_df(-hourg * 0.01 * ssk * massk * r), [&](int dim, const df64 hgf[8]) {
                         // each corner's stress force plus its hourglass force
                         df64 f[8];
                         stress8(dim, f);
