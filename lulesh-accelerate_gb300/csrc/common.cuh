@@ -193,6 +193,40 @@ __device__ __forceinline__ FaceNeighbours face_neighbours(const Dom &d, const De
             __ldg(d.letap + k), __ldg(d.lzetam + k), __ldg(d.lzetap + k)};
 }
 
+// Node n's corner slots (corner * ne + element), in the order of the
+// reference's node-to-corner lists (AllocateNodeElemIndexes,
+// LULESH-OMP.cc:209-268: the node's elements in increasing order), each
+// passed to f(slot, first).  On the structured s^3 cube (Dom::s > 0) they
+// are formed from the node's coordinates -- the element below, behind and
+// left of the node first -- instead of loaded from the corner tables, which
+// takes the tables' loads and their dependent level off the node update.
+template <class F>
+__device__ __forceinline__ void for_node_corners(const Dom &d, int n, F &&f)
+{
+    if (d.s > 0) {
+        const int s = d.s, en = s + 1;
+        const size_t ne = (size_t)d.ne;
+        const int c = n % en, r = (n / en) % en, p = n / (en * en);
+        bool first = true;
+#pragma unroll
+        for (int dp = 1; dp >= 0; --dp)
+#pragma unroll
+            for (int dr = 1; dr >= 0; --dr)
+#pragma unroll
+                for (int dc = 1; dc >= 0; --dc) {
+                    const int ep = p - dp, er = r - dr, ec = c - dc;
+                    if (ep < 0 || ep >= s || er < 0 || er >= s || ec < 0 || ec >= s) continue;
+                    // the node is the corner at offset (dc, dr, dp) of its element
+                    const int corner = dp ? (dr ? (dc ? 6 : 7) : (dc ? 5 : 4)) : (dr ? (dc ? 2 : 3) : (dc ? 1 : 0));
+                    f((int)(corner * ne + (size_t)((ep * s + er) * s + ec)), first);
+                    first = false;
+                }
+        return;
+    }
+    const int st = __ldg(d.corner_start + n), en = __ldg(d.corner_start + n + 1);
+    for (int i = st; i < en; ++i) f(__ldg(d.corner_list + i), i == st);
+}
+
 // One direction of the monotonic limiter (:2198-2228).
 template <typename T>
 __device__ __forceinline__ T limiter_phi(const T *__restrict__ delv, int i, int bm, int bp,

@@ -214,20 +214,18 @@ __device__ __forceinline__ void node_update_df(const Dom &d, int n, const DevSca
     const float2 *cx = reinterpret_cast<const float2 *>(d.fcx);
     const float2 *cy = reinterpret_cast<const float2 *>(d.fcy);
     const float2 *cz = reinterpret_cast<const float2 *>(d.fcz);
-    const int st = __ldg(d.corner_start + n), en = __ldg(d.corner_start + n + 1);
     df64 fx(0.f, 0.f), fy(0.f, 0.f), fz(0.f, 0.f);
-    if (st < en) {
-        const int c = __ldg(d.corner_list + st);
-        fx = as_df(cx[c]);
-        fy = as_df(cy[c]);
-        fz = as_df(cz[c]);
-    }
-    for (int i = st + 1; i < en; ++i) {
-        const int c = __ldg(d.corner_list + i);
-        fx = fx + as_df(cx[c]);
-        fy = fy + as_df(cy[c]);
-        fz = fz + as_df(cz[c]);
-    }
+    for_node_corners(d, n, [&](int c, bool first) {
+        if (first) {
+            fx = as_df(cx[c]);
+            fy = as_df(cy[c]);
+            fz = as_df(cz[c]);
+        } else {
+            fx = fx + as_df(cx[c]);
+            fy = fy + as_df(cy[c]);
+            fz = fz + as_df(cz[c]);
+        }
+    });
     node_integrate(d, n, sc, to_double(fx), to_double(fy), to_double(fz));
 }
 

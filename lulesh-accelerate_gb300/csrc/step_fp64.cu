@@ -233,23 +233,21 @@ __global__ void __launch_bounds__(kBlockElem, 4) k_elem_force(const __grid_const
 __device__ __forceinline__ void node_update_fp64(const Dom &d, int n, const DevScalars *sc)
 {
 
-    const int st = __ldg(d.corner_start + n), en = __ldg(d.corner_start + n + 1);
     // the sums start from the first corner rather than from 0.0 (the same
     // value: x + 0.0 == x, up to the sign of a zero sum), one FP64 add fewer
     // per component; every node belongs to at least one element
     double fx = 0.0, fy = 0.0, fz = 0.0;
-    if (st < en) {
-        const int c = __ldg(d.corner_list + st);
-        fx = d.fcx[c];
-        fy = d.fcy[c];
-        fz = d.fcz[c];
-    }
-    for (int i = st + 1; i < en; ++i) {
-        const int c = __ldg(d.corner_list + i);
-        fx += d.fcx[c];
-        fy += d.fcy[c];
-        fz += d.fcz[c];
-    }
+    for_node_corners(d, n, [&](int c, bool first) {
+        if (first) {
+            fx = d.fcx[c];
+            fy = d.fcy[c];
+            fz = d.fcz[c];
+        } else {
+            fx += d.fcx[c];
+            fy += d.fcy[c];
+            fz += d.fcz[c];
+        }
+    });
     node_integrate(d, n, sc, fx, fy, fz);
 }
 

@@ -378,14 +378,12 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
 __device__ __forceinline__ void node_update_split(const Dom &d, int n, const DevScalars *sc)
 {
 
-    const int st = __ldg(d.corner_start + n), en = __ldg(d.corner_start + n + 1);
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-    for (int i = st; i < en; ++i) {
-        const int c = __ldg(d.corner_list + i);
+    for_node_corners(d, n, [&](int c, bool) {
         kahan_add(sx, cx, d.f32x[c]);
         kahan_add(sy, cy, d.f32y[c]);
         kahan_add(sz, cz, d.f32z[c]);
-    }
+    });
     const double fx = f2d(sx) - f2d(cx);
     const double fy = f2d(sy) - f2d(cy);
     const double fz = f2d(sz) - f2d(cz);
