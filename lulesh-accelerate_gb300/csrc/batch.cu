@@ -643,6 +643,7 @@ int lulesh_batch_create(int n, const int *sizes, const double *e0_scale, int ini
         h.hydro_key = ~0ULL;
         h.elem_begin = (int)eo_i;
         h.edge = sizes[i];
+        h.node_begin = (int)no_i;
         iee_h[i] = (int)(eo_i + nei);
         ine_h[i] = (int)(no_i + nni);
         cpos += 8 * nei;

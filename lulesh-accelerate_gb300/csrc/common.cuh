@@ -196,16 +196,21 @@ __device__ __forceinline__ FaceNeighbours face_neighbours(const Dom &d, const De
 // Node n's corner slots (corner * ne + element), in the order of the
 // reference's node-to-corner lists (AllocateNodeElemIndexes,
 // LULESH-OMP.cc:209-268: the node's elements in increasing order), each
-// passed to f(slot, first).  On the structured s^3 cube (Dom::s > 0) they
-// are formed from the node's coordinates -- the element below, behind and
-// left of the node first -- instead of loaded from the corner tables, which
-// takes the tables' loads and their dependent level off the node update.
+// passed to f(slot, first).  On the structured s^3 cube (Dom::s > 0, or a
+// batch instance's DevScalars::edge > 0, whose nodes and elements are
+// contiguous from node_begin and elem_begin) they are formed from the
+// node's coordinates -- the element below, behind and left of the node
+// first -- instead of loaded from the corner tables, which takes the
+// tables' loads and their dependent level off the node update.
 template <class F>
-__device__ __forceinline__ void for_node_corners(const Dom &d, int n, F &&f)
+__device__ __forceinline__ void for_node_corners(const Dom &d, const DevScalars *sc, int n, F &&f)
 {
-    if (d.s > 0) {
-        const int s = d.s, en = s + 1;
+    const int s = d.s > 0 ? d.s : sc->edge;
+    if (s > 0) {
+        const int en = s + 1;
         const size_t ne = (size_t)d.ne;
+        const int e0 = d.s > 0 ? 0 : sc->elem_begin;
+        if (d.s <= 0) n -= sc->node_begin;
         const int c = n % en, r = (n / en) % en, p = n / (en * en);
         bool first = true;
 #pragma unroll
@@ -218,7 +223,7 @@ __device__ __forceinline__ void for_node_corners(const Dom &d, int n, F &&f)
                     if (ep < 0 || ep >= s || er < 0 || er >= s || ec < 0 || ec >= s) continue;
                     // the node is the corner at offset (dc, dr, dp) of its element
                     const int corner = dp ? (dr ? (dc ? 6 : 7) : (dc ? 5 : 4)) : (dr ? (dc ? 2 : 3) : (dc ? 1 : 0));
-                    f((int)(corner * ne + (size_t)((ep * s + er) * s + ec)), first);
+                    f((int)(corner * ne + (size_t)(e0 + (ep * s + er) * s + ec)), first);
                     first = false;
                 }
         return;

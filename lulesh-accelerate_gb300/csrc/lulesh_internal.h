@@ -46,6 +46,7 @@ struct DevScalars {
     int geo_valid;                       // Dom::geo holds the current positions' geometry
     int elem_begin;                      // first element of the instance (batches)
     int edge;                            // its edge length s, a structured cube (batches; 0 otherwise)
+    int node_begin;                      // its first node (batches)
     unsigned long long courant_key;      // order-preserving keys of the
     unsigned long long hydro_key;        // constraint minima (see keys below)
 };

@@ -215,7 +215,7 @@ __device__ __forceinline__ void node_update_df(const Dom &d, int n, const DevSca
     const float2 *cy = reinterpret_cast<const float2 *>(d.fcy);
     const float2 *cz = reinterpret_cast<const float2 *>(d.fcz);
     df64 fx(0.f, 0.f), fy(0.f, 0.f), fz(0.f, 0.f);
-    for_node_corners(d, n, [&](int c, bool first) {
+    for_node_corners(d, sc, n, [&](int c, bool first) {
         if (first) {
             fx = as_df(cx[c]);
             fy = as_df(cy[c]);

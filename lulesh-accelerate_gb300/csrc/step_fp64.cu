@@ -237,7 +237,7 @@ __device__ __forceinline__ void node_update_fp64(const Dom &d, int n, const DevS
     // value: x + 0.0 == x, up to the sign of a zero sum), one FP64 add fewer
     // per component; every node belongs to at least one element
     double fx = 0.0, fy = 0.0, fz = 0.0;
-    for_node_corners(d, n, [&](int c, bool first) {
+    for_node_corners(d, sc, n, [&](int c, bool first) {
         if (first) {
             fx = d.fcx[c];
             fy = d.fcy[c];

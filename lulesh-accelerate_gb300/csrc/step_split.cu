@@ -379,7 +379,7 @@ __device__ __forceinline__ void node_update_split(const Dom &d, int n, const Dev
 {
 
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-    for_node_corners(d, n, [&](int c, bool) {
+    for_node_corners(d, sc, n, [&](int c, bool) {
         kahan_add(sx, cx, d.f32x[c]);
         kahan_add(sy, cy, d.f32y[c]);
         kahan_add(sz, cz, d.f32z[c]);
